@@ -1,0 +1,181 @@
+"""GB300-native HQRRP: Python mirror of the C ABI in include/hqrrp_gb300.h.
+
+The product is ``libhqrrp_gb300.so`` (C host driver + sm_103a CUDA kernels).
+This module only loads it with ctypes and offers numpy / torch-facing calls
+that mirror the reference's two entry points
+(``lapack_compatible_sources/NoFLA_HQRRP_WY_blk_var4.c``: ``dgeqp4`` :127-300,
+``NoFLA_HQRRP_WY_blk_var4`` :303-571) with the same argument meaning and error
+behaviour.  There is no CPU fallback: if the library is missing or the GPU
+fails, calls raise.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libhqrrp_gb300.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "hqrrp_gb300.h")
+
+PLAIN, MIXED = 0, 1
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_lib = None
+
+
+class HQRRPError(RuntimeError):
+    """A device or shape error reported by libhqrrp_gb300.so."""
+
+
+def build(force=False):
+    """Compile libhqrrp_gb300.so for sm_103a (nvcc); returns its path."""
+    from . import buildlib as _b
+    return _b.build(force=force)
+
+
+def load():
+    """Load libhqrrp_gb300.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise HQRRPError("libhqrrp_gb300.so not built (run hqrrp_gb300.build() / "
+                         "__graft_entry__.build())")
+    L = C.CDLL(LIB_PATH, mode=C.RTLD_LOCAL)
+    L.dgeqp4.argtypes = [_ip, _ip, _dp, _ip, _ip, _dp, _dp, _ip, _ip]
+    L.dgeqp4.restype = None
+    L.NoFLA_HQRRP_WY_blk_var4.argtypes = [C.c_int, C.c_int, _dp, C.c_int, _ip, _dp, C.c_int,
+                                          C.c_int, C.c_int]
+    L.NoFLA_HQRRP_WY_blk_var4.restype = C.c_int
+    L.hqrrp_gb300_set_precision.argtypes = [C.c_int]
+    L.hqrrp_gb300_set_precision.restype = C.c_int
+    L.hqrrp_gb300_set_seed.argtypes = [C.c_ulonglong]
+    L.hqrrp_gb300_set_seed.restype = None
+    L.hqrrp_gb300_set_spin_limit.argtypes = [C.c_uint]
+    L.hqrrp_gb300_set_spin_limit.restype = None
+    L.hqrrp_gb300_hqrrp_sketch.argtypes = [C.c_int, C.c_int, _dp, C.c_int, _ip, _dp, C.c_int,
+                                           C.c_int, C.c_int, _dp, C.c_int]
+    L.hqrrp_gb300_hqrrp_sketch.restype = C.c_int
+    L.hqrrp_gb300_hqrrp_device.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p,
+                                           C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p,
+                                           C.c_int, C.c_ulonglong, C.c_void_p]
+    L.hqrrp_gb300_hqrrp_device.restype = C.c_int
+    L.hqrrp_gb300_dgeqp4_device.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p,
+                                            C.c_void_p, C.c_void_p]
+    L.hqrrp_gb300_dgeqp4_device.restype = C.c_int
+    L.hqrrp_gb300_last_error.argtypes = []
+    L.hqrrp_gb300_last_error.restype = C.c_char_p
+    _lib = L
+    return L
+
+
+def declared_symbols(header=HEADER):
+    """Function names declared in include/hqrrp_gb300.h."""
+    import re
+    text = open(header).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return re.findall(r"\b([A-Za-z_][A-Za-z0-9_]*)\s*\(", text.split("extern \"C\" {", 1)[-1])
+
+
+def last_error():
+    return load().hqrrp_gb300_last_error().decode()
+
+
+def set_precision(mode):
+    return load().hqrrp_gb300_set_precision(int(mode))
+
+
+def set_seed(seed):
+    load().hqrrp_gb300_set_seed(int(seed))
+
+
+def set_spin_limit(limit):
+    load().hqrrp_gb300_set_spin_limit(int(limit))
+
+
+def _fortran(A):
+    return np.array(np.asarray(A, dtype=np.float64), order="F", copy=True)
+
+
+def hqrrp(A, nb=64, pp=10, panel_pivoting=1, jpvt=None, G=None):
+    """NoFLA_HQRRP_WY_blk_var4 on a copy of A (host arrays through the C ABI).
+
+    Returns (A_out, jpvt, tau).  jpvt defaults to 1..n and is carried like the
+    reference carries it.  G: optional explicit sketch ((nb+pp) x m)."""
+    L = load()
+    A = _fortran(A)
+    m, n = A.shape
+    jp = (np.arange(1, n + 1, dtype=np.int32) if jpvt is None
+          else np.array(jpvt, dtype=np.int32, copy=True))
+    tau = np.zeros(max(1, min(m, n)), dtype=np.float64)
+    if G is None:
+        rc = L.NoFLA_HQRRP_WY_blk_var4(m, n, A.ctypes.data_as(_dp), max(1, m),
+                                       jp.ctypes.data_as(_ip), tau.ctypes.data_as(_dp),
+                                       nb, pp, panel_pivoting)
+    else:
+        G = _fortran(G)
+        rc = L.hqrrp_gb300_hqrrp_sketch(m, n, A.ctypes.data_as(_dp), max(1, m),
+                                        jp.ctypes.data_as(_ip), tau.ctypes.data_as(_dp), nb, pp,
+                                        panel_pivoting, G.ctypes.data_as(_dp), G.shape[0])
+    if rc != 0:
+        raise HQRRPError("hqrrp failed (%d): %s" % (rc, last_error()))
+    return A, jp, tau[:min(m, n)]
+
+
+def dgeqp4(A, jpvt=None, lwork=None):
+    """dgeqp4 on a copy of A; returns (A_out, jpvt, tau, info, work0).
+
+    info < 0 is an argument error (as LAPACK); info > 1000 raises."""
+    L = load()
+    A = _fortran(A)
+    m, n = A.shape
+    jp = (np.zeros(n, dtype=np.int32) if jpvt is None
+          else np.array(jpvt, dtype=np.int32, copy=True))
+    tau = np.zeros(max(1, min(m, n)), dtype=np.float64)
+    if lwork is None:
+        lwork = max(1, 3 * n + 1, 2 * n + (n + 1) * 32)
+    work = np.zeros(max(1, lwork), dtype=np.float64)
+    mi, ni, ldi, lw, info = (C.c_int(m), C.c_int(n), C.c_int(max(1, m)), C.c_int(lwork),
+                             C.c_int(0))
+    L.dgeqp4(C.byref(mi), C.byref(ni), A.ctypes.data_as(_dp), C.byref(ldi),
+             jp.ctypes.data_as(_ip), tau.ctypes.data_as(_dp), work.ctypes.data_as(_dp),
+             C.byref(lw), C.byref(info))
+    if info.value > 1000:
+        raise HQRRPError("dgeqp4 failed (info=%d): %s" % (info.value, last_error()))
+    return A, jp, tau[:min(m, n)], info.value, work[0]
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        import torch
+        return torch.cuda.current_stream().cuda_stream
+    return int(getattr(stream, "cuda_stream", stream))
+
+
+def hqrrp_device(At, jpvt, tau, nb=64, pp=10, panel_pivoting=1, Gt=None, seed=12, stream=None):
+    """HQRRP on torch CUDA tensors, in place.
+
+    At: (n, m) contiguous float64 = column-major m x n A (ld = m).
+    jpvt: int32 (n,), carried.  tau: float64 (min(m,n),).
+    Gt: optional (m, nb+pp) contiguous float64 = column-major sketch."""
+    L = load()
+    n, m = At.shape
+    assert At.is_contiguous() and At.dtype.is_floating_point
+    gptr = Gt.data_ptr() if Gt is not None else None
+    rc = L.hqrrp_gb300_hqrrp_device(m, n, At.data_ptr(), max(1, m), jpvt.data_ptr(),
+                                    tau.data_ptr(), nb, pp, panel_pivoting, gptr,
+                                    nb + pp, int(seed), _stream_ptr(stream))
+    if rc != 0:
+        raise HQRRPError("hqrrp_device failed (%d): %s" % (rc, last_error()))
+
+
+def dgeqp4_device(At, jpvt, tau, stream=None):
+    """dgeqp4 on torch CUDA tensors (At: (n, m) contiguous = column-major A)."""
+    L = load()
+    n, m = At.shape
+    info = L.hqrrp_gb300_dgeqp4_device(m, n, At.data_ptr(), max(1, m), jpvt.data_ptr(),
+                                       tau.data_ptr(), _stream_ptr(stream))
+    if info > 1000:
+        raise HQRRPError("dgeqp4_device failed (info=%d): %s" % (info, last_error()))
+    return info

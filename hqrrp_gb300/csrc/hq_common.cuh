@@ -1,0 +1,117 @@
+// hq_common.cuh -- device helpers shared by the HQRRP kernels (sm_103a).
+//
+// Grid-wide barriers here are bounded: every spin has an iteration cap, after
+// which the waiting CTA records an error code in the call's error word and
+// returns, so a barrier that can never complete ends the kernel instead of
+// hanging the GPU.  The host reads the error word after the call.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "hq_internal.h"
+
+#define HQ_WARP 32
+
+__device__ __forceinline__ unsigned hq_ld_acquire(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void hq_red_release_add(unsigned* p, unsigned v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ int hq_ld_volatile(const int* p) {
+  return *(const volatile int*)p;
+}
+
+// Loads that bypass L1: data written by other CTAs during this kernel.
+__device__ __forceinline__ double hq_ldcg(const double* p) { return __ldcg(p); }
+__device__ __forceinline__ int hq_ldcg(const int* p) { return __ldcg(p); }
+
+// Bounded grid barrier.  `counter` is zeroed before the launch; barrier number
+// `epoch` (1-based) completes when the counter reaches epoch * nctas.  Returns
+// false (in every thread of the CTA) if the wait gave up or another CTA
+// reported an error; the caller must then leave the kernel.
+__device__ __forceinline__ bool hq_grid_barrier(unsigned* counter, int* err, unsigned epoch,
+                                                unsigned spin_limit, int* s_flag) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    hq_red_release_add(counter, 1u);
+    const unsigned target = epoch * gridDim.x;
+    unsigned spins = 0;
+    int ok = 1;
+    while (hq_ld_acquire(counter) < target) {
+      if (hq_ld_volatile(err) != 0) {
+        ok = 0;
+        break;
+      }
+      if (++spins > spin_limit) {
+        atomicCAS(err, 0, HQ_ERR_BARRIER_TIMEOUT);
+        ok = 0;
+        break;
+      }
+      __nanosleep(32);
+    }
+    *s_flag = ok;
+  }
+  __syncthreads();
+  return *s_flag != 0;
+}
+
+template <typename T>
+__device__ __forceinline__ T hq_warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// sqrt(a^2 + b^2) without destructive overflow (LAPACK DLAPY2's formula).
+__device__ __forceinline__ double hq_lapy2(double a, double b) {
+  double x = fabs(a), y = fabs(b);
+  double w = fmax(x, y), z = fmin(x, y);
+  if (z == 0.0 || isnan(a) || isnan(b)) return (isnan(a) || isnan(b)) ? a + b : w;
+  double q = z / w;
+  return w * sqrt(1.0 + q * q);
+}
+
+// Householder generation in the convention of LAPACK DLARFG: given alpha and
+// the norm of the tail x, returns tau, beta (the new alpha) and the factor
+// the tail is scaled by so that v = [1; scale * x].  tau == 0 means H = I.
+// The safe-minimum rescaling loop of DLARFG only changes results for columns
+// whose norm is below ~1e-292; it is reproduced by scaling beta and alpha.
+struct HqReflector {
+  double tau, beta, scale;
+};
+
+__device__ __forceinline__ HqReflector hq_make_reflector(double alpha, double xnorm) {
+  HqReflector r;
+  if (xnorm == 0.0) {
+    r.tau = 0.0;
+    r.beta = alpha;
+    r.scale = 1.0;
+    return r;
+  }
+  const double safmin = 2.2250738585072014e-308 / 1.1102230246251565e-16;  // dlamch S / E
+  const double rsafmn = 1.0 / safmin;
+  double beta = -copysign(hq_lapy2(alpha, xnorm), alpha);
+  int knt = 0;
+  double a = alpha, xn = xnorm, mul = 1.0;
+  while (fabs(beta) < safmin && knt < 20) {
+    ++knt;
+    mul *= rsafmn;
+    a *= rsafmn;
+    xn *= rsafmn;
+    beta = -copysign(hq_lapy2(a, xn), a);
+  }
+  r.tau = (beta - a) / beta;
+  r.scale = mul / (a - beta);
+  for (int k = 0; k < knt; ++k) beta *= safmin;
+  r.beta = beta;
+  return r;
+}
+
+// LAPACK's tol3z = sqrt(dlamch('Epsilon')) with eps = 2^-53.
+#define HQ_TOL3Z 1.0536712127723509e-08

@@ -1,0 +1,91 @@
+/* hq_internal.h -- internal launcher interface between the C host driver
+ * (hqrrp_driver.c) and the CUDA kernels (*.cu).  Plain C: no CUDA types beyond
+ * cudaStream_t, no torch.  Every launcher enqueues work on `stream` and returns
+ * a cudaError_t-compatible int (0 = success) for the launch itself; errors
+ * found by the kernels are written to the device error word of the call.
+ */
+#ifndef HQ_INTERNAL_H
+#define HQ_INTERNAL_H
+
+#include <cuda_runtime_api.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Device error codes written by kernels (never collide with cudaError_t
+ * values, which the driver reports separately). */
+#define HQ_ERR_BARRIER_TIMEOUT 0x4801 /* a grid barrier or flag wait gave up */
+#define HQ_ERR_BAD_SHAPE 0x4802       /* a kernel got a shape it cannot take */
+
+/* Limits of the kernels. */
+#define HQ_MAX_MY 256    /* nb + pp (rows of the sketch) */
+#define HQ_MAX_PANEL 1024 /* columns of one pivoted panel kernel */
+
+typedef struct hq_device_info {
+  int device;
+  int num_sms;
+  size_t smem_optin; /* max dynamic shared memory per CTA */
+} hq_device_info;
+
+int hq_query_device(hq_device_info* info);
+
+/* ---- FP64 GEMM: C = alpha * op(A) * op(B) + beta * C (column-major) ---- */
+/* ws: scratch for split-K partial sums (ws_elems doubles; may be NULL). */
+int hq_dgemm(cudaStream_t stream, const hq_device_info* dev, char transa, char transb, int M,
+             int N, int K, double alpha, const double* A, int lda, const double* B, int ldb,
+             double beta, double* Cm, int ldc, double* ws, size_t ws_elems);
+
+/* ---- Gaussian sketch: G (rows x cols, ld) ~ N(0,1) from Philox4x32-10 ---- */
+int hq_sketch_philox(cudaStream_t stream, int rows, int cols, double* G, int ldg,
+                     unsigned long long seed);
+
+/* ---- Pivot selection: b-stage pivoted QR of the mY x N sketch -----------
+ * Reads Y (mY x N, ldy); when the columns do not fit in the shared memory of
+ * the grid, V (same shape, ldv) is used as a working copy.  Writes the final
+ * column permutation as (dst, src) pairs: pairs[2*i], pairs[2*i+1], count in
+ * *npairs (zeroed by the launcher). */
+int hq_skinny_qrp(cudaStream_t stream, const hq_device_info* dev, int mY, int N, int b,
+                  const double* Y, int ldy, double* V, int ldv, int* pairs, int* npairs,
+                  double* part, size_t part_elems, unsigned* bar, int* err,
+                  unsigned spin_limit);
+size_t hq_skinny_part_elems(const hq_device_info* dev, int mY);
+
+/* ---- Panel: pivoted (or plain) QR of the mp x nc block P (ldp) ---------
+ * In place: R on and above the diagonal, Householder vectors below it.
+ * tau[0..nc), U (mp x nc, ldu) = explicit unit-lower copy of the vectors,
+ * perm[k] = source column of final column k. */
+int hq_panel_qrp(cudaStream_t stream, const hq_device_info* dev, int mp, int nc, int pivoting,
+                 double* P, int ldp, double* tau, double* U, int ldu,
+                 int* perm, double* part, size_t part_elems, double* rowbuf, unsigned* bar,
+                 int* err, unsigned spin_limit);
+size_t hq_panel_part_elems(const hq_device_info* dev, int nc);
+
+/* ---- T factor of a forward columnwise block reflector (DLARFT) -----------
+ * Z = U^T U (k x k, ldz) is given; writes T (k x k, ldt), zero below the
+ * diagonal. */
+int hq_larft_from_gram(cudaStream_t stream, int k, const double* Z, int ldz, const double* tau,
+                       double* T, int ldt);
+
+/* ---- Column permutation by (dst, src) pairs -----------------------------
+ * For rows 0..rows-1 of X (ldx): X[:, dst] = X_old[:, src] for each pair, via
+ * tmp (rows x max_pairs, ldt = rows).  Labels (int, may be NULL) are
+ * permuted the same way. */
+int hq_permute_pairs(cudaStream_t stream, int rows, double* X, int ldx, const int* pairs,
+                     const int* npairs, int max_pairs, double* tmp, int* labels,
+                     int* label_tmp);
+
+/* Apply a permutation of nc columns given as perm[k] = source column. */
+int hq_permute_cols(cudaStream_t stream, int rows, double* X, int ldx, int nc, const int* perm,
+                    double* tmp, int* labels, int* label_tmp);
+
+/* ---- Small kernels ---- */
+int hq_fill_iota(cudaStream_t stream, int* x, int n, int base);
+int hq_copy_matrix(cudaStream_t stream, int rows, int cols, const double* src, int lds,
+                   double* dst, int ldd);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,654 @@
+/* hqrrp_driver.c -- host side of libhqrrp_gb300.so (C99).
+ *
+ * The host only validates arguments, moves data, allocates device workspace
+ * from a library-owned stream-ordered pool and enqueues kernels; every
+ * arithmetic step of the factorization runs on the GPU.  The block loop of
+ * HQRRP (lapack_compatible_sources/NoFLA_HQRRP_WY_blk_var4.c:412-558) is
+ * enqueued without any host synchronisation: pivots, permutations and
+ * reflectors stay on the device, and the host waits once at the end.
+ */
+#include <cuda_runtime_api.h>
+#include <pthread.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "hq_internal.h"
+#include "hqrrp_gb300.h"
+
+#define HQ_API __attribute__((visibility("default")))
+
+enum {
+  HQ_OK = 0,
+  HQ_E_CUDA = 1,        /* a CUDA call failed */
+  HQ_E_DEVICE = 2,      /* a kernel reported an error (barrier timeout, ...) */
+  HQ_E_UNSUPPORTED = 3, /* shape outside the kernels' limits */
+  HQ_E_NOMEM = 4        /* device allocation failed */
+};
+
+#define DGEQP4_SMALL_DGEQP3 1000 /* ...var4.c:58 */
+#define LAPACK_NB_DGEQRF 32 /* ILAENV(1, 'DGEQRF') of reference LAPACK */
+#define FIXED_BLOCK 128
+#define DEFAULT_SPIN_LIMIT (1u << 22)
+
+static __thread char g_err[512];
+static int g_precision = -1;
+static unsigned long long g_seed = 12ULL;
+static unsigned g_spin_limit = 0;
+static pthread_mutex_t g_lock = PTHREAD_MUTEX_INITIALIZER;
+
+typedef struct {
+  int ready;
+  hq_device_info dev;
+  cudaStream_t stream;
+  cudaMemPool_t pool;
+} dev_state;
+static dev_state g_devs[64];
+
+static void set_err(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof g_err, fmt, ap);
+  va_end(ap);
+}
+
+HQ_API const char* hqrrp_gb300_last_error(void) { return g_err; }
+
+HQ_API int hqrrp_gb300_set_precision(int mode) {
+  if (mode != 0 && mode != 1) return -1;
+  int prev = g_precision < 0 ? 0 : g_precision;
+  g_precision = mode;
+  return prev;
+}
+
+HQ_API void hqrrp_gb300_set_seed(unsigned long long seed) { g_seed = seed; }
+
+HQ_API void hqrrp_gb300_set_spin_limit(unsigned limit) { g_spin_limit = limit; }
+
+static int precision(void) {
+  if (g_precision < 0) {
+    const char* e = getenv("HQRRP_GB300_PRECISION");
+    g_precision = (e && strcmp(e, "mixed") == 0) ? 1 : 0;
+  }
+  return g_precision;
+}
+
+static unsigned spin_limit(void) { return g_spin_limit ? g_spin_limit : DEFAULT_SPIN_LIMIT; }
+
+static int imin(int a, int b) { return a < b ? a : b; }
+static int imax(int a, int b) { return a > b ? a : b; }
+static int round_up(int x, int q) { return (x + q - 1) / q * q; }
+
+/* Library state of the current device: stream and memory pool. */
+static dev_state* current_device(void) {
+  int d = 0;
+  cudaError_t e = cudaGetDevice(&d);
+  if (e != cudaSuccess || d < 0 || d >= 64) {
+    set_err("no CUDA device: %s", cudaGetErrorString(e));
+    return NULL;
+  }
+  dev_state* s = &g_devs[d];
+  pthread_mutex_lock(&g_lock);
+  if (!s->ready) {
+    int rc = hq_query_device(&s->dev);
+    if (rc == 0) rc = (int)cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+    if (rc == 0) {
+      struct cudaMemPoolProps props;
+      memset(&props, 0, sizeof props);
+      props.allocType = cudaMemAllocationTypePinned;
+      props.handleTypes = cudaMemHandleTypeNone;
+      props.location.type = cudaMemLocationTypeDevice;
+      props.location.id = d;
+      rc = (int)cudaMemPoolCreate(&s->pool, &props);
+      if (rc == 0) {
+        unsigned long long keep = ~0ULL;
+        cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+      }
+    }
+    if (rc != 0) {
+      set_err("device initialisation failed: %s", cudaGetErrorString((cudaError_t)rc));
+      pthread_mutex_unlock(&g_lock);
+      return NULL;
+    }
+    s->ready = 1;
+  }
+  pthread_mutex_unlock(&g_lock);
+  return s;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Device workspace of one call.                                            */
+
+#define MAX_ALLOCS 32
+typedef struct {
+  dev_state* ds;
+  cudaStream_t st;
+  void* ptrs[MAX_ALLOCS];
+  int nptr;
+  int failed;
+  /* HQRRP buffers */
+  double *G, *Y, *V, *U, *T, *Z, *W1, *W2, *Bm, *B2, *ws, *part, *rowbuf, *tmp;
+  int *pairs, *npairs, *perm, *labels, *label_tmp, *err;
+  unsigned* bar;
+  int ldg, ldy, ldu, ldw, ldt, ldz, ldb, tmp_rows, tmp_cols;
+  size_t ws_elems, part_elems;
+} hq_ws;
+
+static void* ws_alloc(hq_ws* w, size_t bytes) {
+  void* p = NULL;
+  if (w->failed) return NULL;
+  if (bytes == 0) bytes = 16;
+  cudaError_t e = cudaMallocFromPoolAsync(&p, bytes, w->ds->pool, w->st);
+  if (e != cudaSuccess || w->nptr >= MAX_ALLOCS) {
+    set_err("device allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+    w->failed = 1;
+    return NULL;
+  }
+  w->ptrs[w->nptr++] = p;
+  return p;
+}
+
+static void ws_release(hq_ws* w) {
+  for (int i = 0; i < w->nptr; ++i) cudaFreeAsync(w->ptrs[i], w->st);
+  w->nptr = 0;
+}
+
+#define CK(call)                                                                  \
+  do {                                                                            \
+    int rc_ = (int)(call);                                                        \
+    if (rc_ != 0) {                                                               \
+      set_err("%s failed: %s", #call, cudaGetErrorString((cudaError_t)rc_));      \
+      return HQ_E_CUDA;                                                           \
+    }                                                                             \
+  } while (0)
+
+/* Workspace for HQRRP on an m x n matrix with block nb + oversampling pp,
+ * and for the pivoted / unpivoted panels of dgeqp4 (panel width <= pw). */
+static int ws_setup(hq_ws* w, int m, int n, int nb, int pp, int pw) {
+  const hq_device_info* dev = &w->ds->dev;
+  const int mY = nb + pp;
+  const int kmax = imax(nb, pw);
+  w->ldg = round_up(imax(mY, 1), 2);
+  w->ldy = w->ldg;
+  w->ldb = w->ldg;
+  w->ldu = round_up(imax(m, 1), 32);
+  w->ldw = imax(kmax, 1);
+  w->ldt = imax(kmax, 1);
+  w->ldz = imax(kmax, 1);
+  w->ws_elems = (size_t)8 << 20;
+  size_t pe = hq_skinny_part_elems(dev, imin(imax(mY, 1), HQ_MAX_MY));
+  size_t pe2 = hq_panel_part_elems(dev, imin(imax(kmax, 1), HQ_MAX_PANEL));
+  w->part_elems = pe > pe2 ? pe : pe2;
+  w->tmp_rows = imax(m, mY);
+  w->tmp_cols = imax(2 * kmax, 1);
+  if (mY > 0) {
+    w->G = ws_alloc(w, sizeof(double) * (size_t)w->ldg * imax(m, 1));
+    w->Y = ws_alloc(w, sizeof(double) * (size_t)w->ldy * imax(n, 1));
+    w->V = ws_alloc(w, sizeof(double) * (size_t)w->ldy * imax(n, 1));
+    w->Bm = ws_alloc(w, sizeof(double) * (size_t)w->ldb * kmax);
+    w->B2 = ws_alloc(w, sizeof(double) * (size_t)w->ldb * kmax);
+  }
+  w->U = ws_alloc(w, sizeof(double) * (size_t)w->ldu * kmax);
+  w->T = ws_alloc(w, sizeof(double) * (size_t)w->ldt * kmax);
+  w->Z = ws_alloc(w, sizeof(double) * (size_t)w->ldz * kmax);
+  w->W1 = ws_alloc(w, sizeof(double) * (size_t)w->ldw * imax(n, 1));
+  w->W2 = ws_alloc(w, sizeof(double) * (size_t)w->ldw * imax(n, 1));
+  w->ws = ws_alloc(w, sizeof(double) * w->ws_elems);
+  w->part = ws_alloc(w, sizeof(double) * w->part_elems);
+  w->rowbuf = ws_alloc(w, sizeof(double) * 2 * (size_t)imax(kmax, 1));
+  w->tmp = ws_alloc(w, sizeof(double) * (size_t)w->tmp_rows * w->tmp_cols);
+  w->pairs = ws_alloc(w, sizeof(int) * 4 * (size_t)kmax);
+  w->npairs = ws_alloc(w, sizeof(int) * 2);
+  w->perm = ws_alloc(w, sizeof(int) * (size_t)kmax);
+  w->labels = ws_alloc(w, sizeof(int) * (size_t)imax(n, 1));
+  w->label_tmp = ws_alloc(w, sizeof(int) * (size_t)imax(n, 2 * kmax));
+  w->err = ws_alloc(w, sizeof(int) * 2);
+  w->bar = ws_alloc(w, sizeof(unsigned) * 2);
+  if (w->failed) return HQ_E_NOMEM;
+  CK(cudaMemsetAsync(w->err, 0, sizeof(int) * 2, w->st));
+  return HQ_OK;
+}
+
+/* Read the device error word; 0 if clean. */
+static int ws_check(hq_ws* w) {
+  int herr = 0;
+  CK(cudaMemcpyAsync(&herr, w->err, sizeof(int), cudaMemcpyDeviceToHost, w->st));
+  CK(cudaStreamSynchronize(w->st));
+  if (herr != 0) {
+    set_err("device kernel reported error 0x%x%s", herr,
+            herr == HQ_ERR_BARRIER_TIMEOUT ? " (grid barrier wait gave up)" : "");
+    return HQ_E_DEVICE;
+  }
+  return HQ_OK;
+}
+
+#define DG(ta, tb, M, N, K, al, A, lda, B, ldb, be, C, ldc)                              \
+  CK(hq_dgemm(w->st, dev, ta, tb, M, N, K, al, A, lda, B, ldb, be, C, ldc, w->ws,       \
+              w->ws_elems))
+
+/* Build T for the b reflectors in U (mp rows) and apply Q^T from the left to
+ * C (mp x nc2): the dlarfb('L','T','F','C') of ...var4.c:711-740. */
+static int block_reflector(hq_ws* w, int mp, int b, const double* tau, double* Cm, int ldc,
+                           int nc2) {
+  const hq_device_info* dev = &w->ds->dev;
+  DG('T', 'N', b, b, mp, 1.0, w->U, w->ldu, w->U, w->ldu, 0.0, w->Z, w->ldz);
+  CK(hq_larft_from_gram(w->st, b, w->Z, w->ldz, tau, w->T, w->ldt));
+  if (nc2 > 0) {
+    DG('T', 'N', b, nc2, mp, 1.0, w->U, w->ldu, Cm, ldc, 0.0, w->W1, w->ldw);
+    DG('T', 'N', b, nc2, b, 1.0, w->T, w->ldt, w->W1, w->ldw, 0.0, w->W2, w->ldw);
+    DG('N', 'N', mp, nc2, b, -1.0, w->U, w->ldu, w->W2, w->ldw, 1.0, Cm, ldc);
+  }
+  return HQ_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* HQRRP block loop (...var4.c:403-558) on device data.                      */
+
+static int core_hqrrp(hq_ws* w, int m, int n, double* dA, int ldda, int* djpvt, double* dtau,
+                      int nb, int pp, int panel_piv, const double* dG, int lddg,
+                      unsigned long long seed) {
+  const hq_device_info* dev = &w->ds->dev;
+  const int mY = nb + pp, mn = imin(m, n);
+  const unsigned spin = spin_limit();
+  if (mn == 0) return HQ_OK;
+
+  /* Sketch G and Y = G A. */
+  if (dG) CK(hq_copy_matrix(w->st, mY, m, dG, lddg, w->G, w->ldg));
+  else CK(hq_sketch_philox(w->st, mY, m, w->G, w->ldg, seed));
+  DG('N', 'N', mY, n, m, 1.0, w->G, w->ldg, dA, ldda, 0.0, w->Y, w->ldy);
+
+  for (int j = 0; j < mn; j += nb) {
+    const int b = imin(nb, imin(n - j, m - j));
+    const int last = (j + nb >= m) || (j + nb >= n);
+    const int mp = m - j, nc2 = imax(0, n - j - b);
+    double* AR = dA + (size_t)j * ldda;
+    double* ABR = AR + j;
+    double* YR = w->Y + (size_t)j * w->ldy;
+
+    if (!last) {
+      /* Pivot selection on the sketch, then one gather of A, Y and jpvt. */
+      CK(hq_skinny_qrp(w->st, dev, mY, n - j, b, YR, w->ldy, w->V, w->ldy, w->pairs, w->npairs,
+                       w->part, w->part_elems, w->bar, w->err, spin));
+      CK(hq_permute_pairs(w->st, m, AR, ldda, w->pairs, w->npairs, 2 * b, w->tmp, djpvt + j,
+                          w->label_tmp));
+      CK(hq_permute_pairs(w->st, mY, YR, w->ldy, w->pairs, w->npairs, 2 * b, w->tmp, NULL,
+                          NULL));
+    }
+
+    /* Panel QR (pivoted within its b columns), U, tau. */
+    CK(hq_panel_qrp(w->st, dev, mp, b, panel_piv, ABR, ldda, dtau + j, w->U, w->ldu, w->perm,
+                    w->part, w->part_elems, w->rowbuf, w->bar + 1, w->err, spin));
+    /* The panel's swaps on the rows above it and on the labels. */
+    CK(hq_permute_cols(w->st, j, AR, ldda, b, w->perm, w->tmp, djpvt + j, w->label_tmp));
+
+    /* T and the trailing update [A12; A22] := Q^T [A12; A22]. */
+    int rc = block_reflector(w, mp, b, dtau + j, ABR + (size_t)b * ldda, ldda, nc2);
+    if (rc) return rc;
+
+    if (!last) {
+      /* Sketch downdate (...var4.c:617-708):
+       *   G_R := G_R (I - U T U^T);  Y2 -= G_R[:, 0:b] R12. */
+      double* GR = w->G + (size_t)j * w->ldg;
+      DG('N', 'N', mY, b, mp, 1.0, GR, w->ldg, w->U, w->ldu, 0.0, w->Bm, w->ldb);
+      DG('N', 'N', mY, b, b, 1.0, w->Bm, w->ldb, w->T, w->ldt, 0.0, w->B2, w->ldb);
+      DG('N', 'T', mY, mp, b, -1.0, w->B2, w->ldb, w->U, w->ldu, 1.0, GR, w->ldg);
+      DG('N', 'N', mY, nc2, b, -1.0, GR, w->ldg, ABR + (size_t)b * ldda, ldda, 1.0,
+         YR + (size_t)b * w->ldy, w->ldy);
+    }
+  }
+  return HQ_OK;
+}
+
+static int check_hqrrp_shape(int nb, int pp) {
+  if (nb < 1 || pp < 0 || nb + pp > HQ_MAX_MY) {
+    set_err("unsupported block parameters nb=%d pp=%d (need nb >= 1, pp >= 0, nb+pp <= %d)", nb,
+            pp, HQ_MAX_MY);
+    return HQ_E_UNSUPPORTED;
+  }
+  return HQ_OK;
+}
+
+static int ws_begin(hq_ws* w, cudaStream_t user_stream, int use_user) {
+  memset(w, 0, sizeof *w);
+  w->ds = current_device();
+  if (!w->ds) return HQ_E_CUDA;
+  w->st = use_user ? user_stream : w->ds->stream;
+  return HQ_OK;
+}
+
+/* Host-pointer HQRRP: copy in, factor, copy out. */
+static int hqrrp_host(int m, int n, double* A, int lda, int* jpvt, double* tau, int nb, int pp,
+                      int panel_piv, const double* G, int ldg) {
+  int rc = check_hqrrp_shape(nb, pp);
+  if (rc) return rc;
+  hq_ws w;
+  if ((rc = ws_begin(&w, NULL, 0))) return rc;
+  const int mn = imin(m, n), mY = nb + pp, ldda = round_up(m, 32);
+  rc = ws_setup(&w, m, n, nb, pp, nb);
+  double* dA = rc ? NULL : ws_alloc(&w, sizeof(double) * (size_t)ldda * n);
+  double* dtau = rc ? NULL : ws_alloc(&w, sizeof(double) * (size_t)mn);
+  int* djp = rc ? NULL : ws_alloc(&w, sizeof(int) * (size_t)n);
+  double* dG = (rc || !G) ? NULL : ws_alloc(&w, sizeof(double) * (size_t)mY * m);
+  if (w.failed) rc = HQ_E_NOMEM;
+  cudaStream_t st = w.st;
+#define CKF(call)                                                            \
+  do {                                                                       \
+    if (!rc) {                                                               \
+      int e_ = (int)(call);                                                  \
+      if (e_) {                                                              \
+        set_err("%s failed: %s", #call, cudaGetErrorString((cudaError_t)e_)); \
+        rc = HQ_E_CUDA;                                                      \
+      }                                                                      \
+    }                                                                        \
+  } while (0)
+  CKF(cudaMemcpy2DAsync(dA, sizeof(double) * ldda, A, sizeof(double) * lda, sizeof(double) * m, n,
+                        cudaMemcpyHostToDevice, st));
+  CKF(cudaMemcpyAsync(djp, jpvt, sizeof(int) * n, cudaMemcpyHostToDevice, st));
+  if (G) CKF(cudaMemcpy2DAsync(dG, sizeof(double) * mY, G, sizeof(double) * ldg,
+                               sizeof(double) * mY, m, cudaMemcpyHostToDevice, st));
+  if (!rc) rc = core_hqrrp(&w, m, n, dA, ldda, djp, dtau, nb, pp, panel_piv, dG, mY, g_seed);
+  if (!rc) rc = ws_check(&w);
+  CKF(cudaMemcpy2DAsync(A, sizeof(double) * lda, dA, sizeof(double) * ldda, sizeof(double) * m, n,
+                        cudaMemcpyDeviceToHost, st));
+  CKF(cudaMemcpyAsync(jpvt, djp, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
+  CKF(cudaMemcpyAsync(tau, dtau, sizeof(double) * mn, cudaMemcpyDeviceToHost, st));
+  ws_release(&w);
+  CKF(cudaStreamSynchronize(st));
+  return rc;
+}
+
+static int hqrrp_args_ok(int m, int n, int lda) {
+  int bad = 0;
+  if (m < 0) { fprintf(stderr, "ERROR in NoFLA_HQRRP_WY_blk_var4: m_A is < 0.\n"); bad = 1; }
+  if (n < 0) { fprintf(stderr, "ERROR in NoFLA_HQRRP_WY_blk_var4: n_A is < 0.\n"); bad = 1; }
+  if (lda < imax(1, m)) {
+    fprintf(stderr, "ERROR in NoFLA_HQRRP_WY_blk_var4: ldim_A is < max( 1, m_A ).\n");
+    bad = 1;
+  }
+  return !bad;
+}
+
+HQ_API int NoFLA_HQRRP_WY_blk_var4(int m_A, int n_A, double* buff_A, int ldim_A, int* buff_jpvt,
+                                   double* buff_tau, int nb_alg, int pp, int panel_pivoting) {
+  g_err[0] = 0;
+  if (!hqrrp_args_ok(m_A, n_A, ldim_A)) return 0;
+  if (imin(m_A, n_A) == 0) return 0;
+  return hqrrp_host(m_A, n_A, buff_A, ldim_A, buff_jpvt, buff_tau, nb_alg, pp, panel_pivoting,
+                    NULL, 0);
+}
+
+HQ_API int hqrrp_gb300_hqrrp_sketch(int m, int n, double* A, int lda, int* jpvt, double* tau,
+                                    int nb, int pp, int panel_pivoting, const double* G, int ldg) {
+  g_err[0] = 0;
+  if (!hqrrp_args_ok(m, n, lda)) return 0;
+  if (imin(m, n) == 0) return 0;
+  if (G == NULL || ldg < nb + pp) {
+    set_err("explicit sketch missing or ldg < nb + pp");
+    return HQ_E_UNSUPPORTED;
+  }
+  return hqrrp_host(m, n, A, lda, jpvt, tau, nb, pp, panel_pivoting, G, ldg);
+}
+
+HQ_API int hqrrp_gb300_hqrrp_device(int m, int n, double* dA, int ldda, int* d_jpvt,
+                                    double* d_tau, int nb, int pp, int panel_pivoting,
+                                    const double* dG, int lddg, unsigned long long seed,
+                                    void* stream) {
+  g_err[0] = 0;
+  if (m < 0 || n < 0 || ldda < imax(1, m)) {
+    set_err("invalid m, n or ldda");
+    return HQ_E_UNSUPPORTED;
+  }
+  if (imin(m, n) == 0) return 0;
+  int rc = check_hqrrp_shape(nb, pp);
+  if (rc) return rc;
+  if (dG && lddg < nb + pp) {
+    set_err("lddg < nb + pp");
+    return HQ_E_UNSUPPORTED;
+  }
+  hq_ws w;
+  if ((rc = ws_begin(&w, (cudaStream_t)stream, 1))) return rc;
+  rc = ws_setup(&w, m, n, nb, pp, nb);
+  if (!rc) rc = core_hqrrp(&w, m, n, dA, ldda, d_jpvt, d_tau, nb, pp, panel_pivoting, dG, lddg, seed);
+  if (!rc) rc = ws_check(&w);
+  ws_release(&w);
+  if (!rc) {
+    int e = (int)cudaStreamSynchronize(w.st);
+    if (e) {
+      set_err("cudaStreamSynchronize failed: %s", cudaGetErrorString((cudaError_t)e));
+      rc = HQ_E_CUDA;
+    }
+  }
+  return rc;
+}
+
+/* ------------------------------------------------------------------------ */
+/* dgeqp4 (...var4.c:127-300) on device data.                                */
+
+/* Move the fixed columns (jpvt != 0) to the front exactly as the reference
+ * does (...var4.c:201-218, the same loop as LAPACK dgeqp3/dgeqpf), returning
+ * their count; hjp is updated in place to 1-based labels and src[k] receives
+ * the original column now at position k. */
+static int fixed_columns_front(int n, int* hjp, int* src) {
+  int nfix = 0;
+  for (int k = 0; k < n; ++k) src[k] = k;
+  for (int c = 0; c < n; ++c) {
+    if (hjp[c] != 0) {
+      if (c != nfix) {
+        int t = src[c];
+        src[c] = src[nfix];
+        src[nfix] = t;
+        hjp[c] = hjp[nfix];
+        hjp[nfix] = c + 1;
+      } else {
+        hjp[c] = c + 1;
+      }
+      ++nfix;
+    } else {
+      hjp[c] = c + 1;
+    }
+  }
+  return nfix;
+}
+
+/* Everything of dgeqp4 after argument checking.  hjp: host copy of jpvt (in:
+ * fixed marks; out: 1-based permutation).  Returns HQ_* and the LAPACK-style
+ * workspace figure in *iws_out. */
+static int core_dgeqp4(hq_ws* w, int m, int n, double* dA, int ldda, int* hjp, int* djp,
+                       double* dtau, int* iws_out) {
+  const hq_device_info* dev = &w->ds->dev;
+  const int mn = imin(m, n);
+  const int small = mn < DGEQP4_SMALL_DGEQP3;
+  const unsigned spin = spin_limit();
+  int iws = 3 * n + 1;
+
+  /* 1. Fixed columns to the front (host bookkeeping, one device gather). */
+  int* src = malloc(sizeof(int) * (size_t)n);
+  int* hpairs = malloc(sizeof(int) * 2 * (size_t)n);
+  if (!src || !hpairs) {
+    free(src);
+    free(hpairs);
+    set_err("host allocation failed");
+    return HQ_E_NOMEM;
+  }
+  const int nfix = fixed_columns_front(n, hjp, src);
+  int np = 0;
+  for (int k = 0; k < n; ++k)
+    if (src[k] != k) {
+      hpairs[2 * np] = k;
+      hpairs[2 * np + 1] = src[k];
+      ++np;
+    }
+  free(src);
+  CK(cudaMemcpyAsync(djp, hjp, sizeof(int) * n, cudaMemcpyHostToDevice, w->st));
+  if (np > 0) {
+    int* dpairs = ws_alloc(w, sizeof(int) * 2 * (size_t)np);
+    double* dtmp = ws_alloc(w, sizeof(double) * (size_t)m * np);
+    if (w->failed) {
+      free(hpairs);
+      return HQ_E_NOMEM;
+    }
+    int rc0 = (int)cudaMemcpyAsync(dpairs, hpairs, sizeof(int) * 2 * np, cudaMemcpyHostToDevice,
+                                   w->st);
+    if (!rc0) rc0 = (int)cudaMemcpyAsync(w->npairs, &np, sizeof(int), cudaMemcpyHostToDevice, w->st);
+    if (!rc0) rc0 = (int)cudaStreamSynchronize(w->st); /* hpairs / np are stack/heap */
+    if (!rc0) rc0 = hq_permute_pairs(w->st, m, dA, ldda, dpairs, w->npairs, np, dtmp, NULL, NULL);
+    if (rc0) {
+      free(hpairs);
+      set_err("fixed-column gather failed: %s", cudaGetErrorString((cudaError_t)rc0));
+      return HQ_E_CUDA;
+    }
+  }
+  free(hpairs);
+
+  /* 2. Unpivoted blocked QR of the fixed columns, updating all columns to
+   *    their right (dgeqrf + dormqr of ...var4.c:220-242). */
+  const int nf = imin(m, nfix);
+  for (int j = 0; j < nf; j += FIXED_BLOCK) {
+    const int b = imin(FIXED_BLOCK, nf - j), mp = m - j;
+    double* ABR = dA + j + (size_t)j * ldda;
+    CK(hq_panel_qrp(w->st, dev, mp, b, 0, ABR, ldda, dtau + j, w->U, w->ldu, w->perm, w->part,
+                    w->part_elems, w->rowbuf, w->bar + 1, w->err, spin));
+    int rc = block_reflector(w, mp, b, dtau + j, ABR + (size_t)b * ldda, ldda, n - j - b);
+    if (rc) return rc;
+  }
+  if (nf > 0) {
+    /* The workspace LAPACK's dgeqrf and dormqr would report (reference
+     * LAPACK 3.x: N*NB and NW*NB + 65*64). */
+    iws = imax(iws, nf * LAPACK_NB_DGEQRF);
+    if (nf < n) iws = imax(iws, (n - nf) * LAPACK_NB_DGEQRF + 65 * 64);
+  }
+
+  /* 3. The free columns: pivoted QR (small path) or HQRRP(64, 10, 1).  The
+   *    permutation of the free block is tracked with position labels and
+   *    then applied to the rows above it and to jpvt (...var4.c:267-292). */
+  if (nf < mn) {
+    const int mt = m - nf, nt = n - nf;
+    double* At = dA + nf + (size_t)nf * ldda;
+    CK(hq_fill_iota(w->st, w->labels, nt, 0));
+    if (small) {
+      if (nt > HQ_MAX_PANEL) {
+        set_err("dgeqp4 small-matrix path supports at most %d free columns (got %d)",
+                HQ_MAX_PANEL, nt);
+        return HQ_E_UNSUPPORTED;
+      }
+      CK(hq_panel_qrp(w->st, dev, mt, nt, 1, At, ldda, dtau + nf, NULL, w->ldu, w->perm,
+                      w->part, w->part_elems, w->rowbuf, w->bar + 1, w->err, spin));
+      CK(hq_permute_cols(w->st, nf, dA + (size_t)nf * ldda, ldda, nt, w->perm, w->tmp,
+                         djp + nf, w->label_tmp));
+    } else {
+      int rc = core_hqrrp(w, mt, nt, At, ldda, w->labels, dtau + nf, 64, 10, 1, NULL, 0, g_seed);
+      if (rc) return rc;
+      double* t2 = w->tmp;
+      if ((size_t)nf * nt > (size_t)w->tmp_rows * w->tmp_cols) {
+        t2 = ws_alloc(w, sizeof(double) * (size_t)nf * nt);
+        if (!t2) return HQ_E_NOMEM;
+      }
+      CK(hq_permute_cols(w->st, nf, dA + (size_t)nf * ldda, ldda, nt, w->labels, t2, djp + nf,
+                         w->label_tmp));
+    }
+  }
+  /* LAPACK's dgeqp3 reports max(LWKOPT, the fixed-column workspace). */
+  if (small) iws = imax(iws, 2 * n + (n + 1) * LAPACK_NB_DGEQRF);
+  *iws_out = iws;
+  return HQ_OK;
+}
+
+static int dgeqp4_ws(hq_ws* w, int m, int n) {
+  const int mn = imin(m, n);
+  if (mn < DGEQP4_SMALL_DGEQP3) {
+    /* pivoted panel of up to n - nf columns plus fixed blocks */
+    int rc = ws_setup(w, m, n, 0, 0, imax(FIXED_BLOCK, imin(n, HQ_MAX_PANEL)));
+    return rc;
+  }
+  return ws_setup(w, m, n, 64, 10, FIXED_BLOCK);
+}
+
+static void xerbla_dgeqp3(int arg) {
+  fprintf(stderr, " ** On entry to DGEQP3 parameter number %2d had an illegal value\n", arg);
+}
+
+/* Argument checks and the workspace query of ...var4.c:148-187.  Returns 1
+ * when the caller should return immediately. */
+static int dgeqp4_prologue(int m, int n, int lda, int lwork, double* work, int* info) {
+  const int mn = imin(m, n), query = (lwork == -1);
+  *info = 0;
+  if (m < 0) *info = -1;
+  else if (n < 0) *info = -2;
+  else if (lda < imax(1, m)) *info = -4;
+  if (*info == 0) {
+    int iws = 1, lwkopt = 1;
+    if (mn != 0) {
+      iws = 3 * n + 1;
+      lwkopt = 2 * n + (n + 1) * LAPACK_NB_DGEQRF;
+    }
+    if (work) work[0] = (double)lwkopt;
+    if (work && lwork < iws && !query) *info = -8;
+  }
+  if (*info != 0) {
+    xerbla_dgeqp3(-*info);
+    return 1;
+  }
+  return query || mn == 0;
+}
+
+HQ_API void dgeqp4(int* m, int* n, double* A, int* lda, int* jpvt, double* tau, double* work,
+                   int* lwork, int* info) {
+  g_err[0] = 0;
+  if (dgeqp4_prologue(*m, *n, *lda, *lwork, work, info)) return;
+  const int M = *m, N = *n, LDA = *lda, mn = imin(M, N), ldda = round_up(M, 32);
+  hq_ws w;
+  int rc = ws_begin(&w, NULL, 0);
+  if (rc) {
+    *info = 1000 + rc;
+    return;
+  }
+  int* hjp = malloc(sizeof(int) * (size_t)N);
+  rc = hjp ? dgeqp4_ws(&w, M, N) : HQ_E_NOMEM;
+  double* dA = rc ? NULL : ws_alloc(&w, sizeof(double) * (size_t)ldda * N);
+  double* dtau = rc ? NULL : ws_alloc(&w, sizeof(double) * (size_t)mn);
+  int* djp = rc ? NULL : ws_alloc(&w, sizeof(int) * (size_t)N);
+  if (!rc && w.failed) rc = HQ_E_NOMEM;
+  cudaStream_t st = w.st;
+  if (hjp) memcpy(hjp, jpvt, sizeof(int) * (size_t)N);
+  CKF(cudaMemcpy2DAsync(dA, sizeof(double) * ldda, A, sizeof(double) * LDA, sizeof(double) * M, N,
+                        cudaMemcpyHostToDevice, st));
+  int iws = 3 * N + 1;
+  if (!rc) rc = core_dgeqp4(&w, M, N, dA, ldda, hjp, djp, dtau, &iws);
+  if (!rc) rc = ws_check(&w);
+  CKF(cudaMemcpy2DAsync(A, sizeof(double) * LDA, dA, sizeof(double) * ldda, sizeof(double) * M, N,
+                        cudaMemcpyDeviceToHost, st));
+  CKF(cudaMemcpyAsync(jpvt, djp, sizeof(int) * N, cudaMemcpyDeviceToHost, st));
+  CKF(cudaMemcpyAsync(tau, dtau, sizeof(double) * mn, cudaMemcpyDeviceToHost, st));
+  ws_release(&w);
+  CKF(cudaStreamSynchronize(st));
+  free(hjp);
+  if (rc) {
+    *info = 1000 + rc;
+    return;
+  }
+  work[0] = (double)iws;
+}
+
+HQ_API int hqrrp_gb300_dgeqp4_device(int m, int n, double* dA, int ldda, int* d_jpvt,
+                                     double* d_tau, void* stream) {
+  g_err[0] = 0;
+  int info = 0;
+  int lw = 3 * (n > 0 ? n : 0) + 1;
+  if (dgeqp4_prologue(m, n, ldda, lw, NULL, &info)) return info;
+  hq_ws w;
+  int rc = ws_begin(&w, (cudaStream_t)stream, 1);
+  if (rc) return 1000 + rc;
+  int* hjp = malloc(sizeof(int) * (size_t)n);
+  rc = hjp ? dgeqp4_ws(&w, m, n) : HQ_E_NOMEM;
+  cudaStream_t st = w.st;
+  CKF(cudaMemcpyAsync(hjp, d_jpvt, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
+  CKF(cudaStreamSynchronize(st));
+  int iws = 0;
+  if (!rc) rc = core_dgeqp4(&w, m, n, dA, ldda, hjp, d_jpvt, d_tau, &iws);
+  if (!rc) rc = ws_check(&w);
+  ws_release(&w);
+  CKF(cudaStreamSynchronize(st));
+  free(hjp);
+  return rc ? 1000 + rc : 0;
+}

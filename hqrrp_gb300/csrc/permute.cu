@@ -1,0 +1,141 @@
+// permute.cu -- column permutations and small utilities.
+//
+// The reference swaps whole columns one pivot at a time with dswap
+// (lapack_compatible_sources/NoFLA_HQRRP_WY_blk_var4.c:990-1036, called from
+// :831-837 for A's m rows, Y and the labels).  Here the b swaps of a block are
+// composed first (by the pivot-selection kernel, as (dst, src) pairs, or by the
+// panel kernel, as perm[k] = src) and applied once: a gather of the moved
+// columns into a scratch buffer, then a scatter to their destinations.  The
+// copies are bit-exact; each moved column is read and written twice, at most
+// 2b columns per block.
+#include "hq_common.cuh"
+
+namespace {
+
+__global__ void gather_pairs(int rows, const double* __restrict__ X, int ldx,
+                             const int* __restrict__ pairs, const int* __restrict__ npairs,
+                             double* __restrict__ tmp, const int* __restrict__ labels,
+                             int* __restrict__ label_tmp) {
+  const int p = blockIdx.y;
+  if (p >= *npairs) return;
+  const int src = pairs[2 * p + 1];
+  const double* s = X + (size_t)src * ldx;
+  double* t = tmp + (size_t)p * rows;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x)
+    t[r] = s[r];
+  if (labels && blockIdx.x == 0 && threadIdx.x == 0) label_tmp[p] = labels[src];
+}
+
+__global__ void scatter_pairs(int rows, double* __restrict__ X, int ldx,
+                              const int* __restrict__ pairs, const int* __restrict__ npairs,
+                              const double* __restrict__ tmp, int* __restrict__ labels,
+                              const int* __restrict__ label_tmp) {
+  const int p = blockIdx.y;
+  if (p >= *npairs) return;
+  const int dst = pairs[2 * p];
+  double* d = X + (size_t)dst * ldx;
+  const double* t = tmp + (size_t)p * rows;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x)
+    d[r] = t[r];
+  if (labels && blockIdx.x == 0 && threadIdx.x == 0) labels[dst] = label_tmp[p];
+}
+
+__global__ void gather_perm(int rows, const double* __restrict__ X, int ldx,
+                            const int* __restrict__ perm, double* __restrict__ tmp,
+                            const int* __restrict__ labels, int* __restrict__ label_tmp) {
+  const int k = blockIdx.y;
+  const int src = perm[k];
+  const double* s = X + (size_t)src * ldx;
+  double* t = tmp + (size_t)k * rows;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x)
+    t[r] = s[r];
+  if (labels && blockIdx.x == 0 && threadIdx.x == 0) label_tmp[k] = labels[src];
+}
+
+__global__ void scatter_perm(int rows, double* __restrict__ X, int ldx,
+                             const double* __restrict__ tmp, int* __restrict__ labels,
+                             const int* __restrict__ label_tmp) {
+  const int k = blockIdx.y;
+  double* d = X + (size_t)k * ldx;
+  const double* t = tmp + (size_t)k * rows;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x)
+    d[r] = t[r];
+  if (labels && blockIdx.x == 0 && threadIdx.x == 0) labels[k] = label_tmp[k];
+}
+
+__global__ void iota_kernel(int* x, int n, int base) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    x[i] = base + i;
+}
+
+__global__ void copy_kernel(int rows, int cols, const double* __restrict__ src, int lds,
+                            double* __restrict__ dst, int ldd) {
+  const size_t total = (size_t)rows * cols;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const int r = (int)(e % rows), c = (int)(e / rows);
+    dst[r + (size_t)c * ldd] = src[r + (size_t)c * lds];
+  }
+}
+
+inline unsigned row_blocks(int rows) {
+  int b = (rows + 255) / 256;
+  if (b > 32) b = 32;
+  return b < 1 ? 1u : (unsigned)b;
+}
+
+}  // namespace
+
+extern "C" int hq_permute_pairs(cudaStream_t stream, int rows, double* X, int ldx,
+                                const int* pairs, const int* npairs, int max_pairs, double* tmp,
+                                int* labels, int* label_tmp) {
+  if (max_pairs <= 0 || (rows <= 0 && labels == nullptr)) return 0;
+  const int r = rows > 0 ? rows : 0;
+  dim3 grid(row_blocks(r), max_pairs);
+  gather_pairs<<<grid, 256, 0, stream>>>(r, X, ldx, pairs, npairs, tmp, labels, label_tmp);
+  scatter_pairs<<<grid, 256, 0, stream>>>(r, X, ldx, pairs, npairs, tmp, labels, label_tmp);
+  return (int)cudaGetLastError();
+}
+
+extern "C" int hq_permute_cols(cudaStream_t stream, int rows, double* X, int ldx, int nc,
+                               const int* perm, double* tmp, int* labels, int* label_tmp) {
+  if (nc <= 0 || (rows <= 0 && labels == nullptr)) return 0;
+  const int r = rows > 0 ? rows : 0;
+  dim3 grid(row_blocks(r), nc);
+  gather_perm<<<grid, 256, 0, stream>>>(r, X, ldx, perm, tmp, labels, label_tmp);
+  scatter_perm<<<grid, 256, 0, stream>>>(r, X, ldx, tmp, labels, label_tmp);
+  return (int)cudaGetLastError();
+}
+
+extern "C" int hq_fill_iota(cudaStream_t stream, int* x, int n, int base) {
+  if (n <= 0) return 0;
+  iota_kernel<<<(n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024, 256, 0, stream>>>(x, n, base);
+  return (int)cudaGetLastError();
+}
+
+extern "C" int hq_copy_matrix(cudaStream_t stream, int rows, int cols, const double* src,
+                              int lds, double* dst, int ldd) {
+  if (rows <= 0 || cols <= 0) return 0;
+  size_t total = (size_t)rows * cols;
+  size_t blocks = (total + 255) / 256;
+  if (blocks > 4096) blocks = 4096;
+  copy_kernel<<<(unsigned)blocks, 256, 0, stream>>>(rows, cols, src, lds, dst, ldd);
+  return (int)cudaGetLastError();
+}
+
+extern "C" int hq_query_device(hq_device_info* info) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return (int)e;
+  int sms = 0, smem = 0;
+  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+    return (int)e;
+  if ((e = cudaDeviceGetAttribute(&smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) !=
+      cudaSuccess)
+    return (int)e;
+  info->device = dev;
+  info->num_sms = sms;
+  // Leave room for the static shared variables of the kernels.
+  info->smem_optin = (size_t)smem - 2048;
+  return 0;
+}

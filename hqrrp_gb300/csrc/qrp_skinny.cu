@@ -1,0 +1,336 @@
+// qrp_skinny.cu -- per-block pivot selection: b stages of pivoted Householder
+// QR on the (nb+pp) x N sketch Y, in one cooperative kernel.
+//
+// Reference: lapack_compatible_sources/NoFLA_HQRRP_WY_blk_var4.c:492-507 copies
+// Y_R into V_R and runs NoFLA_QRPmod_WY_unb_var4 (:774-886) with num_stages =
+// b, which per stage takes idamax of the partial column norms (:828), swaps
+// the columns of V, A, Y and the labels (:831-837, :990-1036), generates and
+// applies a Householder reflector (dlarfg/dlarf, :845-862) and downdates the
+// norms with Drmac's LAWN 176 rule, recomputing them on cancellation
+// (:864-871, :912-986).  Only the pivot sequence leaves this step: V is
+// discarded and the swaps of A, Y and the labels are composed into one
+// permutation that a gather kernel applies afterwards.
+//
+// GB300 layout: the N columns are split into contiguous ranges, one range per
+// CTA (one CTA per SM), and a range stays in that CTA's shared memory for all
+// b stages (138 x 108 doubles = 119 KB at N = 16384, nb = 128), falling back
+// to an L2-resident global copy when it does not fit.  A column never changes
+// owner, so swaps are bookkeeping: each CTA tracks the current position of
+// each of its columns.  Per stage there is ONE grid barrier: each CTA publishes
+// its best candidate (norm, position) together with that column's entries, and
+// after the barrier every CTA picks the same winner (largest norm, lowest
+// position on ties -- BLAS idamax's first-maximum rule) and builds the
+// reflector from the published column itself, so no second exchange is needed.
+#include "hq_common.cuh"
+
+namespace {
+
+constexpr int NT = 256;
+constexpr int NWARP = NT / 32;
+constexpr int MAXT = HQ_MAX_MY / 32;  // row slots per lane
+constexpr int HDR = 4;                // record header: norm, position, column, spare
+
+struct SkArgs {
+  int mY, N, b;
+  const double* Y;
+  int ldy;
+  double* Xg;  // global working copy (global mode)
+  int ldxg;
+  int smem_mode;
+  int nloc_max;
+  int ldxs;
+  int* pairs;
+  int* npairs;
+  double* part;  // [2][P][rec]
+  int rec;
+  unsigned* bar;
+  int* err;
+  unsigned spin_limit;
+};
+
+// Candidate order: larger norm first, then lower position.
+__device__ __forceinline__ bool better(double d1, int p1, double d2, int p2) {
+  return d1 > d2 || (d1 == d2 && p1 < p2);
+}
+
+__global__ void __launch_bounds__(NT, 1) skinny_qrp_kernel(SkArgs a) {
+  extern __shared__ __align__(16) double smem[];
+  const int P = gridDim.x, cta = blockIdx.x, tid = threadIdx.x;
+  const int lane = tid & 31, warp = tid >> 5;
+  const int mY = a.mY;
+  const int c_lo = (int)((long long)cta * a.N / P);
+  const int c_hi = (int)((long long)(cta + 1) * a.N / P);
+  const int nloc = c_hi - c_lo;
+
+  // Shared-memory carve-up.
+  double* sX = smem;
+  double* sd = sX + (a.smem_mode ? (size_t)a.nloc_max * a.ldxs : 0);
+  double* se = sd + a.nloc_max;
+  double* sv = se + a.nloc_max;       // reflector, HQ_MAX_MY
+  double* sred = sv + HQ_MAX_MY;      // 2 * NT scratch
+  int* spos = (int*)(sred + 2 * NT);  // nloc_max
+  int* sint = spos + a.nloc_max;      // small ints
+  __shared__ int s_flag;
+  __shared__ double s_tau;
+  __shared__ int s_win_pos, s_win_cta, s_win_col;
+
+  double* X;
+  int ldx;
+  if (a.smem_mode) {
+    X = sX;
+    ldx = a.ldxs;
+  } else {
+    X = a.Xg + (size_t)c_lo * a.ldxg;
+    ldx = a.ldxg;
+  }
+
+  // Load the range, initialise positions and full column norms.
+  for (int c = warp; c < nloc; c += NWARP) {
+    const double* src = a.Y + (size_t)(c_lo + c) * a.ldy;
+    double* dst = X + (size_t)c * ldx;
+    double q = 0.0;
+    for (int r = lane; r < mY; r += 32) {
+      const double v = src[r];
+      dst[r] = v;
+      q = fma(v, v, q);
+    }
+    q = hq_warp_sum(q);
+    if (lane == 0) {
+      sd[c] = sqrt(q);
+      se[c] = sd[c];
+      spos[c] = c_lo + c;
+    }
+  }
+  __syncthreads();
+
+  unsigned epoch = 0;
+  // Publish this CTA's best candidate for stage s, entries from row s on.
+  auto publish = [&](int s) {
+    double bd = -2.0;
+    int bp = 0x7fffffff, bc = -1;
+    for (int c = tid; c < nloc; c += NT) {
+      if (spos[c] < s) continue;
+      double d = sd[c];
+      if (d != d) d = -1.0;  // NaN never wins over a number
+      if (better(d, spos[c], bd, bp)) { bd = d; bp = spos[c]; bc = c; }
+    }
+    // Block argmax.
+    for (int o = 16; o > 0; o >>= 1) {
+      const double od = __shfl_xor_sync(0xffffffffu, bd, o);
+      const int op = __shfl_xor_sync(0xffffffffu, bp, o);
+      const int oc = __shfl_xor_sync(0xffffffffu, bc, o);
+      if (better(od, op, bd, bp)) { bd = od; bp = op; bc = oc; }
+    }
+    if (lane == 0) {
+      sred[warp] = bd;
+      sint[warp] = bp;
+      sint[NWARP + warp] = bc;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      for (int w = 1; w < NWARP; ++w)
+        if (better(sred[w], sint[w], bd, bp)) { bd = sred[w]; bp = sint[w]; bc = sint[NWARP + w]; }
+      sint[2 * NWARP] = bc;
+      double* rec = a.part + ((size_t)((epoch + 1) & 1) * P + cta) * a.rec;
+      rec[0] = bd;
+      rec[1] = (double)bp;
+      rec[2] = (double)(bc >= 0 ? c_lo + bc : -1);
+    }
+    __syncthreads();
+    const int cbest = sint[2 * NWARP];
+    if (cbest >= 0) {
+      double* rec = a.part + ((size_t)((epoch + 1) & 1) * P + cta) * a.rec;
+      const double* col = X + (size_t)cbest * ldx;
+      for (int r = s + tid; r < mY; r += NT) rec[HDR + r] = col[r];
+    }
+  };
+
+  publish(0);
+  for (int s = 0; s < a.b; ++s) {
+    ++epoch;
+    if (!hq_grid_barrier(a.bar, a.err, epoch, a.spin_limit, &s_flag)) return;
+    const double* recs = a.part + (size_t)(epoch & 1) * P * a.rec;
+
+    // Winner: every CTA reduces the same records in the same way.
+    if (warp == 0) {
+      double bd = -3.0;
+      int bp = 0x7fffffff, bcta = -1;
+      for (int q = lane; q < P; q += 32) {
+        const double d = hq_ldcg(recs + (size_t)q * a.rec);
+        const int p = (int)hq_ldcg(recs + (size_t)q * a.rec + 1);
+        if (d > -2.0 && better(d, p, bd, bp)) { bd = d; bp = p; bcta = q; }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        const double od = __shfl_xor_sync(0xffffffffu, bd, o);
+        const int op = __shfl_xor_sync(0xffffffffu, bp, o);
+        const int oq = __shfl_xor_sync(0xffffffffu, bcta, o);
+        if (better(od, op, bd, bp)) { bd = od; bp = op; bcta = oq; }
+      }
+      if (lane == 0) {
+        s_win_pos = bp;
+        s_win_cta = bcta;
+        s_win_col = bcta >= 0 ? (int)hq_ldcg(recs + (size_t)bcta * a.rec + 2) : -1;
+      }
+    }
+    __syncthreads();
+    const int wpos = s_win_pos, wcta = s_win_cta, wcol = s_win_col;
+    if (wcta < 0) {  // no active column anywhere: cannot happen for b <= N
+      if (tid == 0) atomicCAS(a.err, 0, HQ_ERR_BAD_SHAPE);
+      return;
+    }
+    // Position bookkeeping for the swap of positions s and wpos.
+    if (wpos != s) {
+      for (int c = tid; c < nloc; c += NT)
+        if (spos[c] == s) spos[c] = wpos;
+    }
+    __syncthreads();
+    if (cta == wcta && tid == 0) spos[wcol - c_lo] = s;
+
+    // Reflector from the published winner column (rows s..mY-1).
+    const double* wrec = recs + (size_t)wcta * a.rec + HDR;
+    for (int r = s + tid; r < mY; r += NT) sv[r] = hq_ldcg(wrec + r);
+    __syncthreads();
+    if (warp == 0) {
+      double q = 0.0;
+      for (int r = s + 1 + lane; r < mY; r += 32) q = fma(sv[r], sv[r], q);
+      q = hq_warp_sum(q);
+      if (lane == 0) {
+        const HqReflector h = hq_make_reflector(sv[s], sqrt(q));
+        s_tau = h.tau;
+        sred[0] = h.scale;
+      }
+      __syncwarp();
+      const double scale = sred[0];
+      for (int r = s + 1 + lane; r < mY; r += 32) sv[r] *= scale;
+      if (lane == 0) sv[s] = 1.0;
+    }
+    __syncthreads();
+    if (s + 1 == a.b) break;  // the pivots are complete; V is discarded
+
+    // Apply H = I - tau v v^T to every other active column; downdate norms.
+    const double tau = s_tau;
+    double vr[MAXT];
+#pragma unroll
+    for (int t = 0; t < MAXT; ++t) {
+      const int r = lane + 32 * t;
+      vr[t] = (r >= s && r < mY) ? sv[r] : 0.0;
+    }
+    for (int c = warp; c < nloc; c += NWARP) {
+      if (spos[c] <= s) continue;
+      double* x = X + (size_t)c * ldx;
+      double xr[MAXT];
+      double w = 0.0;
+#pragma unroll
+      for (int t = 0; t < MAXT; ++t) {
+        const int r = lane + 32 * t;
+        xr[t] = (r >= s && r < mY) ? x[r] : 0.0;
+        w = fma(vr[t], xr[t], w);
+      }
+      w = hq_warp_sum(w);
+      const double g = -tau * w;
+      double mine = 0.0;
+#pragma unroll
+      for (int t = 0; t < MAXT; ++t) {
+        const int r = lane + 32 * t;
+        if (r >= s && r < mY) {
+          xr[t] = fma(g, vr[t], xr[t]);
+          x[r] = xr[t];
+        }
+        if (r == s) mine = xr[t];
+      }
+      const double rs = __shfl_sync(0xffffffffu, mine, s & 31);
+      double dc = sd[c];
+      if (dc != 0.0) {
+        double t1 = fabs(rs) / dc;
+        t1 = (1.0 + t1) * (1.0 - t1);
+        if (0.0 > t1) t1 = 0.0;
+        const double ratio = dc / se[c];
+        const double t2 = t1 * ratio * ratio;
+        if (t2 <= HQ_TOL3Z) {
+          double q = 0.0;
+#pragma unroll
+          for (int t = 0; t < MAXT; ++t) {
+            const int r = lane + 32 * t;
+            if (r > s && r < mY) q = fma(xr[t], xr[t], q);
+          }
+          q = hq_warp_sum(q);
+          dc = (mY - s - 1 > 0) ? sqrt(q) : 0.0;
+          if (lane == 0) { sd[c] = dc; se[c] = dc; }
+        } else if (lane == 0) {
+          sd[c] = dc * sqrt(t1);
+        }
+      }
+    }
+    __syncthreads();
+    publish(s + 1);
+  }
+
+  // Final permutation as (dst, src) pairs for the columns that moved.
+  for (int c = tid; c < nloc; c += NT) {
+    if (spos[c] != c_lo + c) {
+      const int i = atomicAdd(a.npairs, 1);
+      a.pairs[2 * i] = spos[c];
+      a.pairs[2 * i + 1] = c_lo + c;
+    }
+  }
+}
+
+int skinny_grid(const hq_device_info* dev, int N) {
+  int p = (N + 15) / 16;
+  if (p > dev->num_sms) p = dev->num_sms;
+  return p < 1 ? 1 : p;
+}
+
+}  // namespace
+
+extern "C" size_t hq_skinny_part_elems(const hq_device_info* dev, int mY) {
+  const int rec = HDR + ((mY + 1) & ~1);
+  return (size_t)2 * dev->num_sms * rec;
+}
+
+extern "C" int hq_skinny_qrp(cudaStream_t stream, const hq_device_info* dev, int mY, int N,
+                             int b, const double* Y, int ldy, double* V, int ldv, int* pairs,
+                             int* npairs, double* part, size_t part_elems, unsigned* bar,
+                             int* err, unsigned spin_limit) {
+  if (mY > HQ_MAX_MY || b > mY || b > N || b <= 0) return (int)cudaErrorInvalidValue;
+  SkArgs a;
+  a.mY = mY;
+  a.N = N;
+  a.b = b;
+  a.Y = Y;
+  a.ldy = ldy;
+  a.Xg = V;
+  a.ldxg = ldv;
+  a.pairs = pairs;
+  a.npairs = npairs;
+  a.part = part;
+  a.rec = HDR + ((mY + 1) & ~1);
+  a.bar = bar;
+  a.err = err;
+  a.spin_limit = spin_limit;
+  const int P = skinny_grid(dev, N);
+  if ((size_t)2 * P * a.rec > part_elems) return (int)cudaErrorInvalidValue;
+  a.nloc_max = (N + P - 1) / P;
+  a.ldxs = mY | 1;
+  const size_t fixed = sizeof(double) * (2 * (size_t)a.nloc_max + HQ_MAX_MY + 2 * NT) +
+                       sizeof(int) * ((size_t)a.nloc_max + 4 * NWARP + 8);
+  const size_t with_x = fixed + sizeof(double) * (size_t)a.nloc_max * a.ldxs;
+  size_t smem;
+  if (with_x <= dev->smem_optin) {
+    a.smem_mode = 1;
+    smem = with_x;
+  } else {
+    a.smem_mode = 0;
+    smem = fixed;
+    if (V == nullptr || smem > dev->smem_optin) return (int)cudaErrorInvalidValue;
+  }
+  cudaError_t e = cudaFuncSetAttribute(skinny_qrp_kernel,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return (int)e;
+  if ((e = cudaMemsetAsync(bar, 0, sizeof(unsigned), stream)) != cudaSuccess) return (int)e;
+  if ((e = cudaMemsetAsync(npairs, 0, sizeof(int), stream)) != cudaSuccess) return (int)e;
+  void* args[] = {&a};
+  e = cudaLaunchCooperativeKernel((const void*)skinny_qrp_kernel, dim3(P), dim3(NT), args, smem,
+                                  stream);
+  return (int)e;
+}

@@ -1,0 +1,96 @@
+/* hqrrp_gb300.h -- C ABI of libhqrrp_gb300.so, the GB300 (sm_103a) HQRRP.
+ *
+ * Householder QR with randomized column pivoting of Martinsson,
+ * Quintana-Orti, Heavner and van de Geijn.  The first two entry points are
+ * drop-in replacements, with identical signatures and argument meaning, for
+ * the reference's C entry points:
+ *
+ *   lapack_compatible_sources/NoFLA_HQRRP_WY_blk_var4.h:1-2   dgeqp4
+ *   lapack_compatible_sources/NoFLA_HQRRP_WY_blk_var4.h:4-6   NoFLA_HQRRP_WY_blk_var4
+ *
+ * All matrices are column-major FP64.  The host-pointer entry points copy A to
+ * the GPU, factor it there and copy A, jpvt and tau back; every arithmetic
+ * step runs in this library's CUDA kernels (no CPU LAPACK).  When the CUDA
+ * device or a kernel fails they report it (info / return code, message from
+ * hqrrp_gb300_last_error()) instead of falling back to the CPU.
+ */
+#ifndef HQRRP_GB300_H
+#define HQRRP_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- Drop-in entry points ------------------------------------------------ */
+
+/* dgeqp3-plug-compatible pivoted QR.  Replaces dgeqp4 of
+ * lapack_compatible_sources/NoFLA_HQRRP_WY_blk_var4.c:127-300.
+ *   jpvt in: jpvt[j] != 0 marks a fixed (leading) column; out: 1-based
+ *   column permutation.  tau: min(m,n) reflector scalars.  work/lwork:
+ *   lwork == -1 is a query (work[0] = 2n + (n+1)*32); otherwise lwork must be
+ *   >= 3n+1 and work[0] returns the workspace LAPACK would report.  work is
+ *   not used as scratch.
+ *   info: 0 ok; -1/-2/-4/-8 as LAPACK (message names DGEQP3, like the
+ *   reference); > 1000 a device error (info - 1000 is the error code, see
+ *   hqrrp_gb300_last_error()).
+ * min(m,n) < 250 follows dgeqpf, < 1000 dgeqp3 (both on the GPU here), larger
+ * matrices HQRRP with nb = 64, pp = 10, panel pivoting on. */
+void dgeqp4(int* m, int* n, double* A, int* lda, int* jpvt, double* tau, double* work,
+            int* lwork, int* info);
+
+/* Blocked HQRRP.  Replaces NoFLA_HQRRP_WY_blk_var4 of
+ * lapack_compatible_sources/NoFLA_HQRRP_WY_blk_var4.c:303-571.
+ *   jpvt is carried: its incoming values are permuted like the columns.
+ *   nb_alg: block size, pp: oversampling (nb_alg + pp <= 256),
+ *   panel_pivoting: 1 = pivoted panel QR, 0 = unpivoted.
+ * Returns 0 on success (always 0 in the reference).  Invalid m, n or lda
+ * print the reference's messages and return 0 without touching A.  A device
+ * error returns its positive code.  The sketch is drawn on the GPU by Philox
+ * (seed hqrrp_gb300_set_seed, default 12), not by libc rand(); the reference's
+ * srand(12) side effect on the caller's rand() state does not happen. */
+int NoFLA_HQRRP_WY_blk_var4(int m_A, int n_A, double* buff_A, int ldim_A, int* buff_jpvt,
+                            double* buff_tau, int nb_alg, int pp, int panel_pivoting);
+
+/* ---- Extensions (no reference counterpart unless stated) ----------------- */
+
+/* Precision of the block updates: 0 = plain FP64 (default), 1 = mixed
+ * (BF16 sketch, split-BF16 tensor-core block updates; FP64 panel, norms,
+ * T).  The environment variable HQRRP_GB300_PRECISION=mixed sets 1.
+ * Returns the previous value, or -1 for an unknown mode. */
+int hqrrp_gb300_set_precision(int mode);
+
+/* Seed of the device Philox sketch used when no sketch is supplied. */
+void hqrrp_gb300_set_seed(unsigned long long seed);
+
+/* Iteration cap of every spin-wait in the cooperative kernels (0 = default).
+ * A wait that reaches it ends the kernel with an error code instead of
+ * hanging; lowering it is how the timeout path is exercised. */
+void hqrrp_gb300_set_spin_limit(unsigned limit);
+
+/* NoFLA_HQRRP_WY_blk_var4 with an explicit host sketch G ((nb+pp) x m,
+ * leading dimension ldg) used in place of the drawn one; with the
+ * reference's own sketch this reproduces the reference run exactly up to
+ * rounding (the oracle feeds it the reference's rand()-based G). */
+int hqrrp_gb300_hqrrp_sketch(int m, int n, double* A, int lda, int* jpvt, double* tau,
+                             int nb, int pp, int panel_pivoting, const double* G, int ldg);
+
+/* Device-pointer HQRRP on `stream` (a cudaStream_t, NULL = legacy default).
+ * dA (ldda >= m), d_jpvt (n ints, carried), d_tau (min(m,n)).  dG: optional
+ * device sketch ((nb+pp) x m, lddg); NULL draws Philox(seed).  Blocks until
+ * the factorization is complete.  Returns 0 or a device error code. */
+int hqrrp_gb300_hqrrp_device(int m, int n, double* dA, int ldda, int* d_jpvt, double* d_tau,
+                             int nb, int pp, int panel_pivoting, const double* dG, int lddg,
+                             unsigned long long seed, void* stream);
+
+/* Device-pointer dgeqp4 (same semantics as dgeqp4; jpvt/tau on the device,
+ * no work array).  Returns info. */
+int hqrrp_gb300_dgeqp4_device(int m, int n, double* dA, int ldda, int* d_jpvt, double* d_tau,
+                              void* stream);
+
+/* Message of the last failure on the calling thread ("" if none). */
+const char* hqrrp_gb300_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
