@@ -64,6 +64,12 @@ def load():
     L.hqrrp_gb300_dgeqp4_device.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p,
                                             C.c_void_p, C.c_void_p]
     L.hqrrp_gb300_dgeqp4_device.restype = C.c_int
+    L.hqrrp_gb300_profile_enable.argtypes = [C.c_int]
+    L.hqrrp_gb300_profile_enable.restype = None
+    L.hqrrp_gb300_profile_read.argtypes = [_dp, _dp, C.c_int]
+    L.hqrrp_gb300_profile_read.restype = C.c_int
+    L.hqrrp_gb300_launch_count.argtypes = []
+    L.hqrrp_gb300_launch_count.restype = C.c_ulonglong
     L.hqrrp_gb300_last_error.argtypes = []
     L.hqrrp_gb300_last_error.restype = C.c_char_p
     _lib = L
@@ -92,6 +98,25 @@ def set_seed(seed):
 
 def set_spin_limit(limit):
     load().hqrrp_gb300_set_spin_limit(int(limit))
+
+
+PHASES = ("sketch", "select", "panel", "update", "downdate", "other")
+
+
+def profile_enable(on=True):
+    load().hqrrp_gb300_profile_enable(1 if on else 0)
+
+
+def profile_read():
+    """{phase: (ms, algorithmic FP64 flops)} since the last read; resets."""
+    ms = np.zeros(8)
+    fl = np.zeros(8)
+    n = load().hqrrp_gb300_profile_read(ms.ctypes.data_as(_dp), fl.ctypes.data_as(_dp), 8)
+    return {PHASES[i]: (float(ms[i]), float(fl[i])) for i in range(n)}
+
+
+def launch_count():
+    return int(load().hqrrp_gb300_launch_count())
 
 
 def _fortran(A):

@@ -162,6 +162,7 @@ extern "C" int hq_dgemm(cudaStream_t stream, const hq_device_info* dev, char tra
   if (K <= 0 || alpha == 0.0) {
     if (beta == 1.0) return 0;
     dgemm_scale<<<dev->num_sms * 4, 256, 0, stream>>>(M, N, beta, Cm, ldc);
+    hq_count_launches(1);
     return (int)cudaGetLastError();
   }
   const bool ta = (transa == 'T' || transa == 't'), tb = (transb == 'T' || transb == 't');
@@ -204,5 +205,6 @@ extern "C" int hq_dgemm(cudaStream_t stream, const hq_device_info* dev, char tra
     if (blocks > dev->num_sms * 8) blocks = dev->num_sms * 8;
     dgemm_splitk_sum<<<blocks, 256, 0, stream>>>(M, N, splits, alpha, ws, beta, Cm, ldc);
   }
+  hq_count_launches(splits > 1 ? 2 : 1);
   return (int)cudaGetLastError();
 }

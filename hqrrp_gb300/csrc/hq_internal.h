@@ -80,6 +80,10 @@ int hq_permute_pairs(cudaStream_t stream, int rows, double* X, int ldx, const in
 int hq_permute_cols(cudaStream_t stream, int rows, double* X, int ldx, int nc, const int* perm,
                     double* tmp, int* labels, int* label_tmp);
 
+/* ---- Launch accounting: every launcher adds the kernels it enqueued ---- */
+void hq_count_launches(int k);
+unsigned long long hq_launches(void);
+
 /* ---- Small kernels ---- */
 int hq_fill_iota(cudaStream_t stream, int* x, int n, int base);
 int hq_copy_matrix(cudaStream_t stream, int rows, int cols, const double* src, int lds,

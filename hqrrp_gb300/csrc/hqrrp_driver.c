@@ -46,6 +46,25 @@ typedef struct {
 } dev_state;
 static dev_state g_devs[64];
 
+/* ---- Per-phase profiler ------------------------------------------------
+ * The libflame variant of the reference accumulates wall-clock time in four
+ * buckets under #ifdef PROFILE (libflame_sources/FLA_HQRRP_UT_blk_var2.c:165-167,
+ * :289-398).  Here the buckets are CUDA-event intervals on the call's stream,
+ * recorded only while profiling is enabled, together with the algorithmic
+ * FP64 flops of the work in each interval. */
+enum { PH_SKETCH = 0, PH_SELECT, PH_PANEL, PH_UPDATE, PH_DOWNDATE, PH_OTHER, PH_COUNT };
+#define PROF_MAXEV 8192
+static int g_prof_on = 0;
+static double g_prof_ms[PH_COUNT], g_prof_flops[PH_COUNT];
+static cudaEvent_t g_prof_ev[PROF_MAXEV];
+static int g_prof_ev_ready = 0;
+
+typedef struct {
+  int n;
+  int ph[PROF_MAXEV];
+  double fl[PROF_MAXEV];
+} prof_rec;
+
 static void set_err(const char* fmt, ...) {
   va_list ap;
   va_start(ap, fmt);
@@ -133,7 +152,60 @@ typedef struct {
   unsigned* bar;
   int ldg, ldy, ldu, ldw, ldt, ldz, ldb, tmp_rows, tmp_cols;
   size_t ws_elems, part_elems;
+  prof_rec* prof; /* non-NULL while profiling */
 } hq_ws;
+
+/* Close the interval since the previous mark and charge it to `phase`. */
+static void prof_mark(hq_ws* w, int phase, double flops) {
+  prof_rec* p = w->prof;
+  if (!p || p->n >= PROF_MAXEV) return;
+  cudaEventRecord(g_prof_ev[p->n], w->st);
+  p->ph[p->n] = phase;
+  p->fl[p->n] = flops;
+  p->n++;
+}
+
+static void prof_start(hq_ws* w) {
+  if (!g_prof_on) return;
+  pthread_mutex_lock(&g_lock);
+  if (!g_prof_ev_ready) {
+    for (int i = 0; i < PROF_MAXEV; ++i) cudaEventCreate(&g_prof_ev[i]);
+    g_prof_ev_ready = 1;
+  }
+  pthread_mutex_unlock(&g_lock);
+  w->prof = calloc(1, sizeof(prof_rec));
+  prof_mark(w, -1, 0.0);
+}
+
+/* After the stream has been synchronised: accumulate the intervals. */
+static void prof_finish(hq_ws* w) {
+  prof_rec* p = w->prof;
+  if (!p) return;
+  for (int i = 1; i < p->n; ++i) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, g_prof_ev[i - 1], g_prof_ev[i]) == cudaSuccess &&
+        p->ph[i] >= 0 && p->ph[i] < PH_COUNT) {
+      g_prof_ms[p->ph[i]] += ms;
+      g_prof_flops[p->ph[i]] += p->fl[i];
+    }
+  }
+  free(p);
+  w->prof = NULL;
+}
+
+HQ_API void hqrrp_gb300_profile_enable(int on) { g_prof_on = on ? 1 : 0; }
+
+HQ_API int hqrrp_gb300_profile_read(double* ms, double* flops, int n) {
+  for (int i = 0; i < PH_COUNT && i < n; ++i) {
+    if (ms) ms[i] = g_prof_ms[i];
+    if (flops) flops[i] = g_prof_flops[i];
+  }
+  memset(g_prof_ms, 0, sizeof g_prof_ms);
+  memset(g_prof_flops, 0, sizeof g_prof_flops);
+  return PH_COUNT;
+}
+
+HQ_API unsigned long long hqrrp_gb300_launch_count(void) { return hq_launches(); }
 
 static void* ws_alloc(hq_ws* w, size_t bytes) {
   void* p = NULL;
@@ -152,6 +224,10 @@ static void* ws_alloc(hq_ws* w, size_t bytes) {
 static void ws_release(hq_ws* w) {
   for (int i = 0; i < w->nptr; ++i) cudaFreeAsync(w->ptrs[i], w->st);
   w->nptr = 0;
+  if (w->prof) { /* an error path skipped ws_check */
+    free(w->prof);
+    w->prof = NULL;
+  }
 }
 
 #define CK(call)                                                                  \
@@ -207,6 +283,7 @@ static int ws_setup(hq_ws* w, int m, int n, int nb, int pp, int pw) {
   w->bar = ws_alloc(w, sizeof(unsigned) * 2);
   if (w->failed) return HQ_E_NOMEM;
   CK(cudaMemsetAsync(w->err, 0, sizeof(int) * 2, w->st));
+  prof_start(w);
   return HQ_OK;
 }
 
@@ -215,6 +292,7 @@ static int ws_check(hq_ws* w) {
   int herr = 0;
   CK(cudaMemcpyAsync(&herr, w->err, sizeof(int), cudaMemcpyDeviceToHost, w->st));
   CK(cudaStreamSynchronize(w->st));
+  prof_finish(w);
   if (herr != 0) {
     set_err("device kernel reported error 0x%x%s", herr,
             herr == HQ_ERR_BARRIER_TIMEOUT ? " (grid barrier wait gave up)" : "");
@@ -234,10 +312,12 @@ static int block_reflector(hq_ws* w, int mp, int b, const double* tau, double* C
   const hq_device_info* dev = &w->ds->dev;
   DG('T', 'N', b, b, mp, 1.0, w->U, w->ldu, w->U, w->ldu, 0.0, w->Z, w->ldz);
   CK(hq_larft_from_gram(w->st, b, w->Z, w->ldz, tau, w->T, w->ldt));
+  prof_mark(w, PH_PANEL, 2.0 * mp * b * b + (double)b * b * b / 3.0);
   if (nc2 > 0) {
     DG('T', 'N', b, nc2, mp, 1.0, w->U, w->ldu, Cm, ldc, 0.0, w->W1, w->ldw);
     DG('T', 'N', b, nc2, b, 1.0, w->T, w->ldt, w->W1, w->ldw, 0.0, w->W2, w->ldw);
     DG('N', 'N', mp, nc2, b, -1.0, w->U, w->ldu, w->W2, w->ldw, 1.0, Cm, ldc);
+    prof_mark(w, PH_UPDATE, 4.0 * mp * b * nc2 + (double)b * b * nc2);
   }
   return HQ_OK;
 }
@@ -257,6 +337,7 @@ static int core_hqrrp(hq_ws* w, int m, int n, double* dA, int ldda, int* djpvt, 
   if (dG) CK(hq_copy_matrix(w->st, mY, m, dG, lddg, w->G, w->ldg));
   else CK(hq_sketch_philox(w->st, mY, m, w->G, w->ldg, seed));
   DG('N', 'N', mY, n, m, 1.0, w->G, w->ldg, dA, ldda, 0.0, w->Y, w->ldy);
+  prof_mark(w, PH_SKETCH, 2.0 * mY * m * n);
 
   for (int j = 0; j < mn; j += nb) {
     const int b = imin(nb, imin(n - j, m - j));
@@ -274,6 +355,9 @@ static int core_hqrrp(hq_ws* w, int m, int n, double* dA, int ldda, int* djpvt, 
                           w->label_tmp));
       CK(hq_permute_pairs(w->st, mY, YR, w->ldy, w->pairs, w->npairs, 2 * b, w->tmp, NULL,
                           NULL));
+      double fl = 0.0;
+      for (int s2 = 0; s2 < b; ++s2) fl += 4.0 * (mY - s2) * (n - j - s2 - 1);
+      prof_mark(w, PH_SELECT, fl);
     }
 
     /* Panel QR (pivoted within its b columns), U, tau. */
@@ -281,6 +365,11 @@ static int core_hqrrp(hq_ws* w, int m, int n, double* dA, int ldda, int* djpvt, 
                     w->part, w->part_elems, w->rowbuf, w->bar + 1, w->err, spin));
     /* The panel's swaps on the rows above it and on the labels. */
     CK(hq_permute_cols(w->st, j, AR, ldda, b, w->perm, w->tmp, djpvt + j, w->label_tmp));
+    {
+      double fl = 0.0;
+      for (int s2 = 0; s2 < b; ++s2) fl += 4.0 * (mp - s2) * (b - s2 - 1);
+      prof_mark(w, PH_PANEL, fl);
+    }
 
     /* T and the trailing update [A12; A22] := Q^T [A12; A22]. */
     int rc = block_reflector(w, mp, b, dtau + j, ABR + (size_t)b * ldda, ldda, nc2);
@@ -295,6 +384,7 @@ static int core_hqrrp(hq_ws* w, int m, int n, double* dA, int ldda, int* djpvt, 
       DG('N', 'T', mY, mp, b, -1.0, w->B2, w->ldb, w->U, w->ldu, 1.0, GR, w->ldg);
       DG('N', 'N', mY, nc2, b, -1.0, GR, w->ldg, ABR + (size_t)b * ldda, ldda, 1.0,
          YR + (size_t)b * w->ldy, w->ldy);
+      prof_mark(w, PH_DOWNDATE, 4.0 * mY * mp * b + 2.0 * mY * b * b + 2.0 * mY * b * nc2);
     }
   }
   return HQ_OK;

@@ -94,6 +94,7 @@ extern "C" int hq_permute_pairs(cudaStream_t stream, int rows, double* X, int ld
   dim3 grid(row_blocks(r), max_pairs);
   gather_pairs<<<grid, 256, 0, stream>>>(r, X, ldx, pairs, npairs, tmp, labels, label_tmp);
   scatter_pairs<<<grid, 256, 0, stream>>>(r, X, ldx, pairs, npairs, tmp, labels, label_tmp);
+  hq_count_launches(2);
   return (int)cudaGetLastError();
 }
 
@@ -104,12 +105,14 @@ extern "C" int hq_permute_cols(cudaStream_t stream, int rows, double* X, int ldx
   dim3 grid(row_blocks(r), nc);
   gather_perm<<<grid, 256, 0, stream>>>(r, X, ldx, perm, tmp, labels, label_tmp);
   scatter_perm<<<grid, 256, 0, stream>>>(r, X, ldx, tmp, labels, label_tmp);
+  hq_count_launches(2);
   return (int)cudaGetLastError();
 }
 
 extern "C" int hq_fill_iota(cudaStream_t stream, int* x, int n, int base) {
   if (n <= 0) return 0;
   iota_kernel<<<(n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024, 256, 0, stream>>>(x, n, base);
+  hq_count_launches(1);
   return (int)cudaGetLastError();
 }
 
@@ -120,8 +123,15 @@ extern "C" int hq_copy_matrix(cudaStream_t stream, int rows, int cols, const dou
   size_t blocks = (total + 255) / 256;
   if (blocks > 4096) blocks = 4096;
   copy_kernel<<<(unsigned)blocks, 256, 0, stream>>>(rows, cols, src, lds, dst, ldd);
+  hq_count_launches(1);
   return (int)cudaGetLastError();
 }
+
+static unsigned long long g_launches = 0;
+
+extern "C" void hq_count_launches(int k) { __atomic_add_fetch(&g_launches, (unsigned long long)k, __ATOMIC_RELAXED); }
+
+extern "C" unsigned long long hq_launches(void) { return __atomic_load_n(&g_launches, __ATOMIC_RELAXED); }
 
 extern "C" int hq_query_device(hq_device_info* info) {
   int dev = 0;

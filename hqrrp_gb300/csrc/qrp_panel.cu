@@ -423,6 +423,7 @@ extern "C" int hq_panel_qrp(cudaStream_t stream, const hq_device_info* dev, int 
   void* args[] = {&a};
   e = cudaLaunchCooperativeKernel((const void*)panel_qrp_kernel, dim3(G), dim3(NT), args, smem,
                                   stream);
+  hq_count_launches(1);
   return (int)e;
 }
 
@@ -439,5 +440,6 @@ extern "C" int hq_larft_from_gram(cudaStream_t stream, int k, const double* Z, i
   } else {
     larft_kernel<<<1, 256, 0, stream>>>(k, Z, ldz, tau, T, ldt, 0);
   }
+  hq_count_launches(1);
   return (int)cudaGetLastError();
 }

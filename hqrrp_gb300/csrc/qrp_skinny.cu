@@ -332,5 +332,6 @@ extern "C" int hq_skinny_qrp(cudaStream_t stream, const hq_device_info* dev, int
   void* args[] = {&a};
   e = cudaLaunchCooperativeKernel((const void*)skinny_qrp_kernel, dim3(P), dim3(NT), args, smem,
                                   stream);
+  hq_count_launches(1);
   return (int)e;
 }

@@ -80,5 +80,6 @@ extern "C" int hq_sketch_philox(cudaStream_t stream, int rows, int cols, double*
   uint64_t blocks = (pairs + 255) / 256;
   if (blocks > 4096) blocks = 4096;
   sketch_philox_kernel<<<(unsigned)blocks, 256, 0, stream>>>(rows, cols, G, ldg, seed);
+  hq_count_launches(1);
   return (int)cudaGetLastError();
 }

@@ -87,6 +87,20 @@ int hqrrp_gb300_hqrrp_device(int m, int n, double* dA, int ldda, int* d_jpvt, do
 int hqrrp_gb300_dgeqp4_device(int m, int n, double* dA, int ldda, int* d_jpvt, double* d_tau,
                               void* stream);
 
+/* Per-phase profiler (off by default).  While enabled, every call records
+ * CUDA events at phase boundaries on its stream; read returns the summed
+ * milliseconds and algorithmic FP64 flops per phase and resets them.  Phases:
+ * 0 sketch + Y = G A, 1 pivot selection (sketch QRP + gathers), 2 panel QR +
+ * T, 3 trailing update (dlarfb), 4 sketch downdate, 5 other.  The reference's
+ * libflame variant keeps the same buckets under #ifdef PROFILE
+ * (libflame_sources/FLA_HQRRP_UT_blk_var2.c:165-167, :289-398).  Returns the
+ * number of phases. */
+void hqrrp_gb300_profile_enable(int on);
+int hqrrp_gb300_profile_read(double* ms, double* flops, int n);
+
+/* Number of kernels this library has launched in this process. */
+unsigned long long hqrrp_gb300_launch_count(void);
+
 /* Message of the last failure on the calling thread ("" if none). */
 const char* hqrrp_gb300_last_error(void);
 
