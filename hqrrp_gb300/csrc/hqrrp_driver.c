@@ -75,7 +75,7 @@ static void set_err(const char* fmt, ...) {
 HQ_API const char* hqrrp_gb300_last_error(void) { return g_err; }
 
 HQ_API int hqrrp_gb300_set_precision(int mode) {
-  if (mode != 0 && mode != 1) return -1;
+  if (mode != 0) return -1; /* only the plain FP64 kernels are built so far */
   int prev = g_precision < 0 ? 0 : g_precision;
   g_precision = mode;
   return prev;

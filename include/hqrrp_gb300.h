@@ -53,10 +53,8 @@ int NoFLA_HQRRP_WY_blk_var4(int m_A, int n_A, double* buff_A, int ldim_A, int* b
 
 /* ---- Extensions (no reference counterpart unless stated) ----------------- */
 
-/* Precision of the block updates: 0 = plain FP64 (default), 1 = mixed
- * (BF16 sketch, split-BF16 tensor-core block updates; FP64 panel, norms,
- * T).  The environment variable HQRRP_GB300_PRECISION=mixed sets 1.
- * Returns the previous value, or -1 for an unknown mode. */
+/* Precision of the block updates: 0 = plain FP64 (default).  Returns the
+ * previous value, or -1 for a mode this build does not provide. */
 int hqrrp_gb300_set_precision(int mode);
 
 /* Seed of the device Philox sketch used when no sketch is supplied. */
