@@ -84,6 +84,11 @@ int hq_permute_cols(cudaStream_t stream, int rows, double* X, int ldx, int nc, c
 void hq_count_launches(int k);
 unsigned long long hq_launches(void);
 
+/* ---- Host driver services for launchers that are entry points ---------- */
+void hq_set_error(const char* fmt, ...);
+void hq_clear_error(void);
+unsigned hq_spin_limit(void);
+
 /* ---- Small kernels ---- */
 int hq_fill_iota(cudaStream_t stream, int* x, int n, int base);
 int hq_copy_matrix(cudaStream_t stream, int rows, int cols, const double* src, int lds,

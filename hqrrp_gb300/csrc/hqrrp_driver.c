@@ -95,6 +95,17 @@ static int precision(void) {
 
 static unsigned spin_limit(void) { return g_spin_limit ? g_spin_limit : DEFAULT_SPIN_LIMIT; }
 
+void hq_set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof g_err, fmt, ap);
+  va_end(ap);
+}
+
+void hq_clear_error(void) { g_err[0] = 0; }
+
+unsigned hq_spin_limit(void) { return spin_limit(); }
+
 static int imin(int a, int b) { return a < b ? a : b; }
 static int imax(int a, int b) { return a > b ? a : b; }
 static int round_up(int x, int q) { return (x + q - 1) / q * q; }

@@ -85,6 +85,22 @@ int hqrrp_gb300_hqrrp_device(int m, int n, double* dA, int ldda, int* d_jpvt, do
 int hqrrp_gb300_dgeqp4_device(int m, int n, double* dA, int ldda, int* d_jpvt, double* d_tau,
                               void* stream);
 
+/* Pivoted QR (LAPACK dgeqp3 results for free columns: R and reflectors in
+ * dA, tau, 1-based jpvt) of an m x n device matrix with n <= 256, that
+ * allocates NO device memory.  No counterpart in the reference.  For callers
+ * that cannot allocate at this point: a process that has given all device
+ * memory to its own arena, or a loop that cannot afford the device
+ * synchronisation of cudaMalloc/cudaFree or their failure under memory
+ * pressure.  Its scratch is a fixed 650 KiB __device__ array held by every GPU
+ * that loads the library until exit, shared by all calls: calls that overlap
+ * on the GPU race and must be serialised by the caller.  The first call on a
+ * device does a one-time set-up (scratch address lookup) and should come
+ * before any stream capture.  Returns 0, 3 for n > 256 or invalid sizes (see
+ * hqrrp_gb300_last_error()), 2 if the kernel reported an error, 1 for a CUDA
+ * error.  Blocks until done. */
+int hqrrp_gb300_qrp_noalloc(int m, int n, double* dA, int ldda, int* d_jpvt, double* d_tau,
+                            void* stream);
+
 /* Per-phase profiler (off by default).  While enabled, every call records
  * CUDA events at phase boundaries on its stream; read returns the summed
  * milliseconds and algorithmic FP64 flops per phase and resets them.  Phases:
