@@ -69,12 +69,12 @@ int hq_larft_from_gram(cudaStream_t stream, int k, const double* Z, int ldz, con
                        double* T, int ldt);
 
 /* ---- Column permutation by (dst, src) pairs -----------------------------
- * For rows 0..rows-1 of X (ldx): X[:, dst] = X_old[:, src] for each pair, via
- * tmp (rows x max_pairs, ldt = rows).  Labels (int, may be NULL) are
- * permuted the same way. */
-int hq_permute_pairs(cudaStream_t stream, int rows, double* X, int ldx, const int* pairs,
-                     const int* npairs, int max_pairs, double* tmp, int* labels,
-                     int* label_tmp);
+ * For rows 0..rows-1 of X (ldx, ncols columns): X[:, dst] = X_old[:, src] for
+ * each pair, via tmp (rows x max_pairs, ldt = rows).  Labels (int, may be
+ * NULL) are permuted the same way. */
+int hq_permute_pairs(cudaStream_t stream, int rows, double* X, int ldx, int ncols,
+                     const int* pairs, const int* npairs, int max_pairs, double* tmp,
+                     int* labels, int* label_tmp);
 
 /* Apply a permutation of nc columns given as perm[k] = source column. */
 int hq_permute_cols(cudaStream_t stream, int rows, double* X, int ldx, int nc, const int* perm,

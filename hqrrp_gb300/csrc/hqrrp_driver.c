@@ -362,9 +362,9 @@ static int core_hqrrp(hq_ws* w, int m, int n, double* dA, int ldda, int* djpvt, 
       /* Pivot selection on the sketch, then one gather of A, Y and jpvt. */
       CK(hq_skinny_qrp(w->st, dev, mY, n - j, b, YR, w->ldy, w->V, w->ldy, w->pairs, w->npairs,
                        w->part, w->part_elems, w->bar, w->err, spin));
-      CK(hq_permute_pairs(w->st, m, AR, ldda, w->pairs, w->npairs, 2 * b, w->tmp, djpvt + j,
-                          w->label_tmp));
-      CK(hq_permute_pairs(w->st, mY, YR, w->ldy, w->pairs, w->npairs, 2 * b, w->tmp, NULL,
+      CK(hq_permute_pairs(w->st, m, AR, ldda, n - j, w->pairs, w->npairs, 2 * b, w->tmp,
+                          djpvt + j, w->label_tmp));
+      CK(hq_permute_pairs(w->st, mY, YR, w->ldy, n - j, w->pairs, w->npairs, 2 * b, w->tmp, NULL,
                           NULL));
       double fl = 0.0;
       for (int s2 = 0; s2 < b; ++s2) fl += 4.0 * (mY - s2) * (n - j - s2 - 1);
@@ -593,7 +593,8 @@ static int core_dgeqp4(hq_ws* w, int m, int n, double* dA, int ldda, int* hjp, i
                                    w->st);
     if (!rc0) rc0 = (int)cudaMemcpyAsync(w->npairs, &np, sizeof(int), cudaMemcpyHostToDevice, w->st);
     if (!rc0) rc0 = (int)cudaStreamSynchronize(w->st); /* hpairs / np are stack/heap */
-    if (!rc0) rc0 = hq_permute_pairs(w->st, m, dA, ldda, dpairs, w->npairs, np, dtmp, NULL, NULL);
+    if (!rc0)
+      rc0 = hq_permute_pairs(w->st, m, dA, ldda, n, dpairs, w->npairs, np, dtmp, NULL, NULL);
     if (rc0) {
       free(hpairs);
       set_err("fixed-column gather failed: %s", cudaGetErrorString((cudaError_t)rc0));

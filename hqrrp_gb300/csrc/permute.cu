@@ -12,13 +12,17 @@
 
 namespace {
 
+// Pair lists and permutations come from the pivoting kernels; an index
+// outside [0, ncols) can only follow an aborted run (whose error word the host
+// reports) and is skipped rather than followed.
 __global__ void gather_pairs(int rows, const double* __restrict__ X, int ldx,
                              const int* __restrict__ pairs, const int* __restrict__ npairs,
-                             double* __restrict__ tmp, const int* __restrict__ labels,
-                             int* __restrict__ label_tmp) {
+                             int ncols, double* __restrict__ tmp,
+                             const int* __restrict__ labels, int* __restrict__ label_tmp) {
   const int p = blockIdx.y;
   if (p >= *npairs) return;
   const int src = pairs[2 * p + 1];
+  if (src < 0 || src >= ncols || pairs[2 * p] < 0 || pairs[2 * p] >= ncols) return;
   const double* s = X + (size_t)src * ldx;
   double* t = tmp + (size_t)p * rows;
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x)
@@ -28,11 +32,12 @@ __global__ void gather_pairs(int rows, const double* __restrict__ X, int ldx,
 
 __global__ void scatter_pairs(int rows, double* __restrict__ X, int ldx,
                               const int* __restrict__ pairs, const int* __restrict__ npairs,
-                              const double* __restrict__ tmp, int* __restrict__ labels,
-                              const int* __restrict__ label_tmp) {
+                              int ncols, const double* __restrict__ tmp,
+                              int* __restrict__ labels, const int* __restrict__ label_tmp) {
   const int p = blockIdx.y;
   if (p >= *npairs) return;
   const int dst = pairs[2 * p];
+  if (dst < 0 || dst >= ncols || pairs[2 * p + 1] < 0 || pairs[2 * p + 1] >= ncols) return;
   double* d = X + (size_t)dst * ldx;
   const double* t = tmp + (size_t)p * rows;
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x)
@@ -45,6 +50,7 @@ __global__ void gather_perm(int rows, const double* __restrict__ X, int ldx,
                             const int* __restrict__ labels, int* __restrict__ label_tmp) {
   const int k = blockIdx.y;
   const int src = perm[k];
+  if (src < 0 || src >= (int)gridDim.y) return;
   const double* s = X + (size_t)src * ldx;
   double* t = tmp + (size_t)k * rows;
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x)
@@ -53,9 +59,10 @@ __global__ void gather_perm(int rows, const double* __restrict__ X, int ldx,
 }
 
 __global__ void scatter_perm(int rows, double* __restrict__ X, int ldx,
-                             const double* __restrict__ tmp, int* __restrict__ labels,
-                             const int* __restrict__ label_tmp) {
+                             const int* __restrict__ perm, const double* __restrict__ tmp,
+                             int* __restrict__ labels, const int* __restrict__ label_tmp) {
   const int k = blockIdx.y;
+  if (perm[k] < 0 || perm[k] >= (int)gridDim.y) return;
   double* d = X + (size_t)k * ldx;
   const double* t = tmp + (size_t)k * rows;
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x)
@@ -86,14 +93,15 @@ inline unsigned row_blocks(int rows) {
 
 }  // namespace
 
-extern "C" int hq_permute_pairs(cudaStream_t stream, int rows, double* X, int ldx,
+extern "C" int hq_permute_pairs(cudaStream_t stream, int rows, double* X, int ldx, int ncols,
                                 const int* pairs, const int* npairs, int max_pairs, double* tmp,
                                 int* labels, int* label_tmp) {
   if (max_pairs <= 0 || (rows <= 0 && labels == nullptr)) return 0;
   const int r = rows > 0 ? rows : 0;
   dim3 grid(row_blocks(r), max_pairs);
-  gather_pairs<<<grid, 256, 0, stream>>>(r, X, ldx, pairs, npairs, tmp, labels, label_tmp);
-  scatter_pairs<<<grid, 256, 0, stream>>>(r, X, ldx, pairs, npairs, tmp, labels, label_tmp);
+  gather_pairs<<<grid, 256, 0, stream>>>(r, X, ldx, pairs, npairs, ncols, tmp, labels, label_tmp);
+  scatter_pairs<<<grid, 256, 0, stream>>>(r, X, ldx, pairs, npairs, ncols, tmp, labels,
+                                           label_tmp);
   hq_count_launches(2);
   return (int)cudaGetLastError();
 }
@@ -104,7 +112,7 @@ extern "C" int hq_permute_cols(cudaStream_t stream, int rows, double* X, int ldx
   const int r = rows > 0 ? rows : 0;
   dim3 grid(row_blocks(r), nc);
   gather_perm<<<grid, 256, 0, stream>>>(r, X, ldx, perm, tmp, labels, label_tmp);
-  scatter_perm<<<grid, 256, 0, stream>>>(r, X, ldx, tmp, labels, label_tmp);
+  scatter_perm<<<grid, 256, 0, stream>>>(r, X, ldx, perm, tmp, labels, label_tmp);
   hq_count_launches(2);
   return (int)cudaGetLastError();
 }

@@ -80,6 +80,11 @@ __global__ void __launch_bounds__(NT, 1) panel_qrp_kernel(PnArgs a) {
     ldx = a.ldp;
   }
   for (int k = tid; k < nc; k += NT) sperm[k] = k;
+  // A valid permutation is in place before any wait: if a barrier gives up
+  // and the kernel returns early, the gathers that follow still read indices
+  // within range.
+  if (cta == 0)
+    for (int k = tid; k < nc; k += NT) a.perm[k] = k;
   __syncthreads();
 
   unsigned epoch = 0;
@@ -91,31 +96,41 @@ __global__ void __launch_bounds__(NT, 1) panel_qrp_kernel(PnArgs a) {
   // dimension) and their sums are combined in sred in a fixed order; from NT
   // columns up, each thread owns columns tid, tid + NT, ...
 
-  // Sum over CTAs of the published values [0, na) into sw[0..na).
+  // Sum over CTAs of the published values [0, na) into sw[0..na), in a
+  // fixed order.  Loads are issued in batches of RB independent L2 reads per
+  // thread so the reduction costs a few L2 round trips, not one per CTA.
+  constexpr int RB = 32;
   auto reduce_parts = [&](unsigned e, int na) {
     const double* base = part_r(e);
-    if (na >= NT) {
-      for (int q = tid; q < na; q += NT) {
-        double t = 0.0;
-        for (int c = 0; c < G; ++c) t += hq_ldcg(base + (size_t)c * a.pstride + q);
-        sw[q] = t;
+    const int groups = na >= NT ? 1 : NT / na;
+    for (int q0 = 0; q0 < na; q0 += NT) {
+      const int q = q0 + tid % min(na, NT), g = tid / min(na, NT);
+      double t = 0.0;
+      if (g < groups && q < na) {
+        for (int c0 = g; c0 < G; c0 += groups * RB) {
+          double v[RB];
+#pragma unroll
+          for (int u = 0; u < RB; ++u) {
+            const int c = c0 + u * groups;
+            v[u] = c < G ? hq_ldcg(base + (size_t)c * a.pstride + q) : 0.0;
+          }
+#pragma unroll
+          for (int u = 0; u < RB; ++u) t += v[u];
+        }
+      }
+      if (groups == 1) {
+        if (g == 0 && q < na) sw[q] = t;
+      } else {
+        sred[tid] = t;
+        __syncthreads();
+        if (tid < na) {
+          double u = 0.0;
+          for (int gg = 0; gg < groups; ++gg) u += sred[gg * na + tid];
+          sw[tid] = u;
+        }
       }
       __syncthreads();
-      return;
     }
-    const int groups = NT / na;
-    const int q = tid % na, g = tid / na;
-    double t = 0.0;
-    if (g < groups)
-      for (int c = g; c < G; c += groups) t += hq_ldcg(base + (size_t)c * a.pstride + q);
-    sred[tid] = t;
-    __syncthreads();
-    if (tid < na) {
-      double u = 0.0;
-      for (int gg = 0; gg < groups; ++gg) u += sred[gg * na + tid];
-      sw[tid] = u;
-    }
-    __syncthreads();
   };
 
   // Slab-local sums over rows with global index > lo_row of x_i * X[i, k]
@@ -131,7 +146,14 @@ __global__ void __launch_bounds__(NT, 1) panel_qrp_kernel(PnArgs a) {
         if (!use_mask || sflag[k]) {
           const double* xk = X + (size_t)k * ldx;
           const double* xx = xs >= 0 ? X + (size_t)xs * ldx : xk;
-          for (int i = i0; i < nloc; ++i) t = fma(xx[i], xk[i], t);
+          double t1 = 0.0;
+          int i = i0;
+          for (; i + 1 < nloc; i += 2) {
+            t = fma(xx[i], xk[i], t);
+            t1 = fma(xx[i + 1], xk[i + 1], t1);
+          }
+          if (i < nloc) t = fma(xx[i], xk[i], t);
+          t += t1;
         }
         out[q] = t;
       }
@@ -146,7 +168,14 @@ __global__ void __launch_bounds__(NT, 1) panel_qrp_kernel(PnArgs a) {
       if (!use_mask || sflag[k]) {
         const double* xk = X + (size_t)k * ldx;
         const double* xx = xs >= 0 ? X + (size_t)xs * ldx : xk;
-        for (int i = i0 + g; i < nloc; i += groups) t = fma(xx[i], xk[i], t);
+        double t1 = 0.0;
+        int i = i0 + g;
+        for (; i + groups < nloc; i += 2 * groups) {
+          t = fma(xx[i], xk[i], t);
+          t1 = fma(xx[i + groups], xk[i + groups], t1);
+        }
+        if (i < nloc) t = fma(xx[i], xk[i], t);
+        t += t1;
       }
     }
     sred[tid] = t;

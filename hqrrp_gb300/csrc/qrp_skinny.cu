@@ -27,7 +27,6 @@ namespace {
 
 constexpr int NT = 256;
 constexpr int NWARP = NT / 32;
-constexpr int MAXT = HQ_MAX_MY / 32;  // row slots per lane
 constexpr int HDR = 4;                // record header: norm, position, column, spare
 
 struct SkArgs {
@@ -41,6 +40,7 @@ struct SkArgs {
   int ldxs;
   int* pairs;
   int* npairs;
+  int max_pairs;
   double* part;  // [2][P][rec]
   int rec;
   unsigned* bar;
@@ -207,38 +207,27 @@ __global__ void __launch_bounds__(NT, 1) skinny_qrp_kernel(SkArgs a) {
     __syncthreads();
     if (s + 1 == a.b) break;  // the pivots are complete; V is discarded
 
-    // Apply H = I - tau v v^T to every other active column; downdate norms.
+    // Apply H = I - tau v v^T to every other active column and downdate its
+    // norm.  One thread per column: the column's dot product, update, norm
+    // test and (rare) norm recomputation need no cross-lane reduction, and no
+    // FP64 work is repeated across lanes.
     const double tau = s_tau;
-    double vr[MAXT];
-#pragma unroll
-    for (int t = 0; t < MAXT; ++t) {
-      const int r = lane + 32 * t;
-      vr[t] = (r >= s && r < mY) ? sv[r] : 0.0;
-    }
-    for (int c = warp; c < nloc; c += NWARP) {
+    for (int c = tid; c < nloc; c += NT) {
       if (spos[c] <= s) continue;
       double* x = X + (size_t)c * ldx;
-      double xr[MAXT];
-      double w = 0.0;
-#pragma unroll
-      for (int t = 0; t < MAXT; ++t) {
-        const int r = lane + 32 * t;
-        xr[t] = (r >= s && r < mY) ? x[r] : 0.0;
-        w = fma(vr[t], xr[t], w);
+      double w0 = x[s], w1 = 0.0, w2 = 0.0, w3 = 0.0;
+      int r = s + 1;
+      for (; r + 3 < mY; r += 4) {
+        w0 = fma(sv[r], x[r], w0);
+        w1 = fma(sv[r + 1], x[r + 1], w1);
+        w2 = fma(sv[r + 2], x[r + 2], w2);
+        w3 = fma(sv[r + 3], x[r + 3], w3);
       }
-      w = hq_warp_sum(w);
-      const double g = -tau * w;
-      double mine = 0.0;
-#pragma unroll
-      for (int t = 0; t < MAXT; ++t) {
-        const int r = lane + 32 * t;
-        if (r >= s && r < mY) {
-          xr[t] = fma(g, vr[t], xr[t]);
-          x[r] = xr[t];
-        }
-        if (r == s) mine = xr[t];
-      }
-      const double rs = __shfl_sync(0xffffffffu, mine, s & 31);
+      for (; r < mY; ++r) w0 = fma(sv[r], x[r], w0);
+      const double g = -tau * ((w0 + w1) + (w2 + w3));
+      const double rs = x[s] + g;
+      x[s] = rs;
+      for (r = s + 1; r < mY; ++r) x[r] = fma(g, sv[r], x[r]);
       double dc = sd[c];
       if (dc != 0.0) {
         double t1 = fabs(rs) / dc;
@@ -247,16 +236,16 @@ __global__ void __launch_bounds__(NT, 1) skinny_qrp_kernel(SkArgs a) {
         const double ratio = dc / se[c];
         const double t2 = t1 * ratio * ratio;
         if (t2 <= HQ_TOL3Z) {
-          double q = 0.0;
-#pragma unroll
-          for (int t = 0; t < MAXT; ++t) {
-            const int r = lane + 32 * t;
-            if (r > s && r < mY) q = fma(xr[t], xr[t], q);
+          double q0 = 0.0, q1 = 0.0;
+          for (r = s + 1; r + 1 < mY; r += 2) {
+            q0 = fma(x[r], x[r], q0);
+            q1 = fma(x[r + 1], x[r + 1], q1);
           }
-          q = hq_warp_sum(q);
-          dc = (mY - s - 1 > 0) ? sqrt(q) : 0.0;
-          if (lane == 0) { sd[c] = dc; se[c] = dc; }
-        } else if (lane == 0) {
+          if (r < mY) q0 = fma(x[r], x[r], q0);
+          dc = (mY - s - 1 > 0) ? sqrt(q0 + q1) : 0.0;
+          sd[c] = dc;
+          se[c] = dc;
+        } else {
           sd[c] = dc * sqrt(t1);
         }
       }
@@ -269,8 +258,12 @@ __global__ void __launch_bounds__(NT, 1) skinny_qrp_kernel(SkArgs a) {
   for (int c = tid; c < nloc; c += NT) {
     if (spos[c] != c_lo + c) {
       const int i = atomicAdd(a.npairs, 1);
-      a.pairs[2 * i] = spos[c];
-      a.pairs[2 * i + 1] = c_lo + c;
+      if (i < a.max_pairs) {
+        a.pairs[2 * i] = spos[c];
+        a.pairs[2 * i + 1] = c_lo + c;
+      } else {
+        atomicCAS(a.err, 0, HQ_ERR_BAD_SHAPE);  // only after an aborted run
+      }
     }
   }
 }
@@ -303,6 +296,7 @@ extern "C" int hq_skinny_qrp(cudaStream_t stream, const hq_device_info* dev, int
   a.ldxg = ldv;
   a.pairs = pairs;
   a.npairs = npairs;
+  a.max_pairs = 2 * b;
   a.part = part;
   a.rec = HDR + ((mY + 1) & ~1);
   a.bar = bar;
