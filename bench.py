@@ -7,13 +7,16 @@ sigma_i = 10^(-12 i / n), nb = 128, pp = 10, panel pivoting on.  Synthetic,
 seeded; generated on the GPU before the timed region.
 
 One step = one full factorization of a fresh copy of A (the 2.1 GB matrix is
-larger than L2, so nothing carries over between steps).  ``value`` is timed
+larger than L2, so nothing carries over between steps).  The headline is the
+mixed-precision path (split-BF16 tensor-core block updates); the plain FP64
+path is timed the same way in the same run and reported beside it, with both
+residuals.  ``value`` is timed
 with CUDA events on the factorization's stream with A already in HBM;
 ``e2e`` goes through the reference-facing C entry point
 NoFLA_HQRRP_WY_blk_var4 with host (pinned) buffers, so both copies are inside
 its timed region.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision plain|mixed]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision both|mixed|plain]
   python bench.py --impl reference ...   # the reference algorithm on host cores
 
 Under torchrun (N > 1) every rank factors its own matrix (replicas: a single
@@ -46,8 +49,8 @@ def parse():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--precision", default=os.environ.get("HQRRP_GB300_PRECISION", "plain"),
-                   choices=["plain", "mixed"])
+    p.add_argument("--precision", default="both", choices=["both", "mixed", "plain"],
+                   help="both (default): headline = mixed, plain timed alongside")
     p.add_argument("--n", type=int, default=16384)
     p.add_argument("--nb", type=int, default=128)
     p.add_argument("--pp", type=int, default=10)
@@ -250,34 +253,10 @@ def measured_peaks():
         return {}
 
 
-def main():
-    args = parse()
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if args.impl == "reference":
-        run_reference_arm(args)
-        return
-
+def run_arm(hq, precision, At0, At, jp, iota, tau, nb, pp, args, device, dist, local):
+    """Warm up, then time exactly args.steps factorizations (one arm)."""
     import torch
-    import hqrrp_gb300 as hq
-    hq.load()
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
-    device = torch.device("cuda", local)
-    torch.cuda.set_device(device)
-    hq.set_precision(hq.MIXED if args.precision == "mixed" else hq.PLAIN)
-
-    n = m = args.n
-    nb, pp = args.nb, args.pp
-    At0 = make_matrix_gpu(n, args.seed + rank, device)
-    At = torch.empty_like(At0)
-    iota = torch.arange(1, n + 1, dtype=torch.int32, device=device)
-    jp = iota.clone()
-    tau = torch.zeros(min(m, n), dtype=torch.float64, device=device)
+    hq.set_precision(hq.MIXED if precision == "mixed" else hq.PLAIN)
     stream = torch.cuda.current_stream()
 
     def step():
@@ -288,8 +267,6 @@ def main():
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
-
-    # Timed region.
     sampler = ClockSampler(local)
     if dist:
         dist.barrier()
@@ -311,39 +288,93 @@ def main():
         t = torch.tensor([ms], dtype=torch.float64, device=device)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t)
-    ms_per_step = ms / args.steps
-    value = world * flops_qr(m, n) / (ms_per_step * 1e-3) / 1e12
-
-    # Quality of the last factorization.
     res, diag = quality_gpu(At0, At, jp, tau)
-    sig = spectrum(n)
-    ratio = diag / sig
-
-    # Phase profile of one more (untimed) factorization -> roofline.
+    ratio = diag / spectrum(At0.shape[0])
+    # One more (untimed) factorization under the phase profiler.
     hq.profile_enable(True)
     hq.profile_read()
     step()
     torch.cuda.synchronize()
     prof = hq.profile_read()
     hq.profile_enable(False)
-    upd_ms, upd_fl = prof["update"]
-    fp64_peak = fp64_peak_tflops(device)
-    achieved = upd_fl / (upd_ms * 1e-3) / 1e12 if upd_ms > 0 else None
-    roofline = {"bound": "tensor", "pipe": "fp64", "kernel": "dgemm_tile (trailing dlarfb update)",
-                "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-                "frac": achieved / fp64_peak if achieved else None,
-                "peak_source": "cuBLAS DGEMM 8192^3 measured in this run (MEASURED_PEAKS.json "
-                               "has no FP64 figure)",
-                "traffic": None,
-                "phases_ms": {k: round(v[0], 3) for k, v in prof.items()},
-                "phases_tflops": {k: (round(v[1] / (v[0] * 1e-3) / 1e12, 4) if v[0] > 0 else None)
-                                  for k, v in prof.items()}}
+    return {"ms_per_step": ms / args.steps, "launches": launches, "clocks": clocks,
+            "quality": {"residual_est": res, "rkk_over_sigma_min": float(ratio.min()),
+                        "rkk_over_sigma_max": float(ratio.max())},
+            "ratio": ratio, "prof": prof}
+
+
+def phase_table(prof):
+    return ({k: round(v[0], 3) for k, v in prof.items()},
+            {k: (round(v[1] / (v[0] * 1e-3) / 1e12, 4) if v[0] > 0 and v[1] > 0 else None)
+             for k, v in prof.items()})
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference_arm(args)
+        return
+
+    import torch
+    import hqrrp_gb300 as hq
+    hq.load()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    device = torch.device("cuda", local)
+    torch.cuda.set_device(device)
+
+    n = m = args.n
+    nb, pp = args.nb, args.pp
+    At0 = make_matrix_gpu(n, args.seed + rank, device)
+    At = torch.empty_like(At0)
+    iota = torch.arange(1, n + 1, dtype=torch.int32, device=device)
+    jp = iota.clone()
+    tau = torch.zeros(min(m, n), dtype=torch.float64, device=device)
+
+    arms = ["mixed", "plain"] if args.precision == "both" else [args.precision]
+    res = {p: run_arm(hq, p, At0, At, jp, iota, tau, nb, pp, args, device, dist, local)
+           for p in arms}
+    head = arms[0]
+    H = res[head]
+    value = world * flops_qr(m, n) / (H["ms_per_step"] * 1e-3) / 1e12
+    peaks = measured_peaks()
+
+    # Roofline of the dominant kernel of the headline arm, from the live phase
+    # profile: mixed -> ozk_gemm_kernel (BF16 tensor work), plain -> dgemm_tile.
+    if head == "mixed":
+        t_ms, t_fl = H["prof"]["tensor"]
+        peak = peaks.get("bf16_tflops_sustained") or 1700.0
+        achieved = t_fl / (t_ms * 1e-3) / 1e12 if t_ms > 0 else None
+        roofline = {"bound": "tensor", "pipe": "bf16 tcgen05", "kernel": "ozk_gemm_kernel "
+                    "(split-BF16 digit products of the block update and sketch downdate)",
+                    "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                    "frac": achieved / peak if achieved else None,
+                    "peak_source": "bf16_tflops_sustained of measured (MEASURED_PEAKS.json)"
+                    if peaks.get("bf16_tflops_sustained") else "fallback 1.7 PFLOP/s sustained",
+                    "traffic": None}
+    else:
+        u_ms, u_fl = H["prof"]["update"]
+        peak = fp64_peak_tflops(device)
+        achieved = u_fl / (u_ms * 1e-3) / 1e12 if u_ms > 0 else None
+        roofline = {"bound": "tensor", "pipe": "fp64", "kernel": "dgemm_tile (trailing dlarfb update)",
+                    "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                    "frac": achieved / peak if achieved else None,
+                    "peak_source": "cuBLAS DGEMM 8192^3 measured in this run (MEASURED_PEAKS.json "
+                                   "has no FP64 figure)", "traffic": None}
+    roofline["phases_ms"], roofline["phases_tflops"] = phase_table(H["prof"])
 
     # End to end through the reference-facing C entry point, host buffers.
     e2e = None
     if args.e2e_steps > 0:
         import ctypes as C
         L = hq.load()
+        hq.set_precision(hq.MIXED if head == "mixed" else hq.PLAIN)
         host0 = At0.cpu().pin_memory()
         hA = torch.empty_like(host0).pin_memory()
         hjp = torch.empty(n, dtype=torch.int32).pin_memory()
@@ -370,7 +401,8 @@ def main():
         e2e = {"value": world * flops_qr(m, n) / sec / 1e12, "unit": "TFLOP/s",
                "h2d_bytes_per_step": 8 * m * n + 4 * n,
                "d2h_bytes_per_step": 8 * m * n + 4 * n + 8 * min(m, n),
-               "ms_per_step": sec * 1e3, "api": "NoFLA_HQRRP_WY_blk_var4 (host pinned buffers)"}
+               "ms_per_step": sec * 1e3, "precision": head,
+               "api": "NoFLA_HQRRP_WY_blk_var4 (host pinned buffers)"}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -381,24 +413,32 @@ def main():
                "sample": "HQRRP nb=%d pp=%d on m=n=%d, same spectrum, best of 2, %.1f s each"
                          % (nb, pp, args.cpu_n, t)}
 
-    peaks = measured_peaks()
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": H["ms_per_step"],
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                "dtype": "f64", "data": "synthetic",
+                "dtype": "f64" if head == "plain" else "f64 (split-bf16 tensor products)",
+                "data": "synthetic",
                 "config": {"workload": "HQRRP m=n=%d nb=%d pp=%d panel_pivoting=1, "
                                        "A=U diag(10^(-12 i/n)) V^T, Haar U,V" % (n, nb, pp),
-                           "m": m, "n": n, "nb": nb, "pp": pp, "precision": args.precision,
+                           "m": m, "n": n, "nb": nb, "pp": pp, "precision": head,
                            "api": "hqrrp_gb300_hqrrp_device", "parallelism": "replicas%d" % world,
                            "l2": "inputs larger than L2 (%.1f GB matrix per step)"
                                  % (8 * m * n / 1e9)},
-                "quality": {"residual_est": res, "rkk_over_sigma_min": float(ratio.min()),
-                            "rkk_over_sigma_max": float(ratio.max())},
-                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-                "gpu_launches": launches, "clocks": clocks,
+                "quality": H["quality"], "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "gpu_launches": H["launches"], "clocks": H["clocks"], "bwd_ms": None,
                 "measured_peaks": {k: peaks.get(k) for k in ("hbm_gbs", "bf16_tflops",
                                                               "bf16_tflops_sustained")}}
+        if "plain" in res and head != "plain":
+            P = res["plain"]
+            pv = world * flops_qr(m, n) / (P["ms_per_step"] * 1e-3) / 1e12
+            pm, pt = phase_table(P["prof"])
+            line["plain"] = {"value": pv, "ms_per_step": P["ms_per_step"],
+                             "quality": P["quality"], "gpu_launches": P["launches"],
+                             "clocks": P["clocks"], "phases_ms": pm, "phases_tflops": pt}
+            line["mixed_over_plain"] = value / pv
+            r = H["ratio"] / P["ratio"]
+            line["quality"]["rkk_ratio_mixed_over_plain"] = [float(r.min()), float(r.max())]
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

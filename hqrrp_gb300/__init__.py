@@ -70,6 +70,10 @@ def load():
     L.hqrrp_gb300_profile_read.restype = C.c_int
     L.hqrrp_gb300_launch_count.argtypes = []
     L.hqrrp_gb300_launch_count.restype = C.c_ulonglong
+    L.hqrrp_gb300_ozaki_dgemm.argtypes = [C.c_char, C.c_char, C.c_int, C.c_int, C.c_int,
+                                          C.c_double, C.c_void_p, C.c_int, C.c_void_p, C.c_int,
+                                          C.c_double, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
+    L.hqrrp_gb300_ozaki_dgemm.restype = C.c_int
     L.hqrrp_gb300_last_error.argtypes = []
     L.hqrrp_gb300_last_error.restype = C.c_char_p
     _lib = L
@@ -100,7 +104,7 @@ def set_spin_limit(limit):
     load().hqrrp_gb300_set_spin_limit(int(limit))
 
 
-PHASES = ("sketch", "select", "panel", "update", "downdate", "other")
+PHASES = ("sketch", "select", "panel", "update", "downdate", "other", "tensor", "split")
 
 
 def profile_enable(on=True):
@@ -109,9 +113,9 @@ def profile_enable(on=True):
 
 def profile_read():
     """{phase: (ms, algorithmic FP64 flops)} since the last read; resets."""
-    ms = np.zeros(8)
-    fl = np.zeros(8)
-    n = load().hqrrp_gb300_profile_read(ms.ctypes.data_as(_dp), fl.ctypes.data_as(_dp), 8)
+    ms = np.zeros(16)
+    fl = np.zeros(16)
+    n = load().hqrrp_gb300_profile_read(ms.ctypes.data_as(_dp), fl.ctypes.data_as(_dp), 16)
     return {PHASES[i]: (float(ms[i]), float(fl[i])) for i in range(n)}
 
 
@@ -204,3 +208,20 @@ def dgeqp4_device(At, jpvt, tau, stream=None):
     if info > 1000:
         raise HQRRPError("dgeqp4_device failed (info=%d): %s" % (info, last_error()))
     return info
+
+
+def ozaki_dgemm(transa, transb, alpha, At, Bt, beta, Ct, slices=6, stream=None):
+    """C = alpha op(A) op(B) + beta C on torch CUDA tensors holding column-major
+    matrices as their transposes (At: (cols, rows) contiguous, and so on).
+    alpha = +-1, beta in {0, 1}."""
+    L = load()
+    m = Ct.shape[1]
+    n = Ct.shape[0]
+    k = (At.shape[1] if transa in ("T", b"T") else At.shape[0])
+    ta = transa.encode() if isinstance(transa, str) else transa
+    tb = transb.encode() if isinstance(transb, str) else transb
+    rc = L.hqrrp_gb300_ozaki_dgemm(ta, tb, m, n, k, float(alpha), At.data_ptr(), At.shape[1],
+                                   Bt.data_ptr(), Bt.shape[1], float(beta), Ct.data_ptr(),
+                                   Ct.shape[1], int(slices), _stream_ptr(stream))
+    if rc != 0:
+        raise HQRRPError("ozaki_dgemm failed (%d): %s" % (rc, last_error()))

@@ -80,6 +80,20 @@ int hq_permute_pairs(cudaStream_t stream, int rows, double* X, int ldx, int ncol
 int hq_permute_cols(cudaStream_t stream, int rows, double* X, int ldx, int nc, const int* perm,
                     double* tmp, int* labels, int* label_tmp);
 
+/* ---- Split-BF16 (Ozaki) FP64 products on tcgen05 -------------------------
+ * side 0 = M side (128-row tiles), 1 = N side (64-row tiles).  X element
+ * (r, k) at X[r*rs + k*ks]; tiles sized by hq_ozk_tile_bytes; exps needs
+ * rows rounded up to the tile height.  gemm: mode 0 writes sign * X Y^T to C,
+ * mode 1 adds it; C element (r, c) at C[r*crs + c*ccs]; ws (optional) holds
+ * split-K slices for mode 0. */
+size_t hq_ozk_tile_bytes(int rows, int K, int S, int side);
+int hq_ozk_split(cudaStream_t stream, const double* X, long long rs, long long ks, int R, int K,
+                 int S, int side, void* tiles, int* exps);
+int hq_ozk_gemm(cudaStream_t stream, const hq_device_info* dev, int M, int N, int K, int S,
+                const void* Atiles, const int* ea, const void* Btiles, const int* eb, int mode,
+                double sign, double* C, long long crs, long long ccs, double* ws,
+                size_t ws_elems, int* err, unsigned spin_limit);
+
 /* ---- Launch accounting: every launcher adds the kernels it enqueued ---- */
 void hq_count_launches(int k);
 unsigned long long hq_launches(void);

@@ -31,6 +31,8 @@ enum {
 #define LAPACK_NB_DGEQRF 32 /* ILAENV(1, 'DGEQRF') of reference LAPACK */
 #define FIXED_BLOCK 128
 #define DEFAULT_SPIN_LIMIT (1u << 22)
+#define OZK_SLICES 7        /* digits per operand in the mixed block updates */
+#define OZK_SKETCH_SLICES 2 /* the sketch Y = G A only steers pivots */
 
 static __thread char g_err[512];
 static int g_precision = -1;
@@ -52,7 +54,8 @@ static dev_state g_devs[64];
  * :289-398).  Here the buckets are CUDA-event intervals on the call's stream,
  * recorded only while profiling is enabled, together with the algorithmic
  * FP64 flops of the work in each interval. */
-enum { PH_SKETCH = 0, PH_SELECT, PH_PANEL, PH_UPDATE, PH_DOWNDATE, PH_OTHER, PH_COUNT };
+enum { PH_SKETCH = 0, PH_SELECT, PH_PANEL, PH_UPDATE, PH_DOWNDATE, PH_OTHER, PH_TENSOR,
+       PH_SPLIT, PH_COUNT };
 #define PROF_MAXEV 8192
 static int g_prof_on = 0;
 static double g_prof_ms[PH_COUNT], g_prof_flops[PH_COUNT];
@@ -75,7 +78,7 @@ static void set_err(const char* fmt, ...) {
 HQ_API const char* hqrrp_gb300_last_error(void) { return g_err; }
 
 HQ_API int hqrrp_gb300_set_precision(int mode) {
-  if (mode != 0) return -1; /* only the plain FP64 kernels are built so far */
+  if (mode != 0 && mode != 1) return -1;
   int prev = g_precision < 0 ? 0 : g_precision;
   g_precision = mode;
   return prev;
@@ -164,6 +167,9 @@ typedef struct {
   int ldg, ldy, ldu, ldw, ldt, ldz, ldb, tmp_rows, tmp_cols;
   size_t ws_elems, part_elems;
   prof_rec* prof; /* non-NULL while profiling */
+  int mixed;      /* split-BF16 tensor-core block updates */
+  void *ozA, *ozB; /* digit tiles of the two operands of a mixed product */
+  int *ozea, *ozeb;
 } hq_ws;
 
 /* Close the interval since the previous mark and charge it to `phase`. */
@@ -292,6 +298,22 @@ static int ws_setup(hq_ws* w, int m, int n, int nb, int pp, int pw) {
   w->label_tmp = ws_alloc(w, sizeof(int) * (size_t)imax(n, 2 * kmax));
   w->err = ws_alloc(w, sizeof(int) * 2);
   w->bar = ws_alloc(w, sizeof(unsigned) * 2);
+  if (w->mixed && mY > 0) {
+    const int S = OZK_SLICES, S2 = OZK_SKETCH_SLICES;
+    size_t a = hq_ozk_tile_bytes(n, m, S2, 0), b = hq_ozk_tile_bytes(mY, m, S2, 1), t;
+    if ((t = hq_ozk_tile_bytes(kmax, m, S, 0)) > a) a = t;
+    if ((t = hq_ozk_tile_bytes(m, kmax, S, 0)) > a) a = t;
+    if ((t = hq_ozk_tile_bytes(n, kmax, S, 0)) > a) a = t;
+    if ((t = hq_ozk_tile_bytes(n, m, S, 1)) > b) b = t;
+    if ((t = hq_ozk_tile_bytes(n, kmax, S, 1)) > b) b = t;
+    if ((t = hq_ozk_tile_bytes(mY, m, S, 1)) > b) b = t;
+    if ((t = hq_ozk_tile_bytes(mY, kmax, S, 1)) > b) b = t;
+    const int rows = imax(imax(m, n), mY) + 128;
+    w->ozA = ws_alloc(w, a);
+    w->ozB = ws_alloc(w, b);
+    w->ozea = ws_alloc(w, sizeof(int) * (size_t)rows);
+    w->ozeb = ws_alloc(w, sizeof(int) * (size_t)rows);
+  }
   if (w->failed) return HQ_E_NOMEM;
   CK(cudaMemsetAsync(w->err, 0, sizeof(int) * 2, w->st));
   prof_start(w);
@@ -316,6 +338,23 @@ static int ws_check(hq_ws* w) {
   CK(hq_dgemm(w->st, dev, ta, tb, M, N, K, al, A, lda, B, ldb, be, C, ldc, w->ws,       \
               w->ws_elems))
 
+/* sign * X Y^T (mode 0: written to C; mode 1: added to C) with split-BF16
+ * tensor-core products: X has M rows (element (r, k) at X[r*xrs + k*xks]),
+ * Y has N rows, both K long; C element (r, c) at C[r*crs + c*ccs]. */
+static int ozk_product(hq_ws* w, int S, int M, int N, int K, const double* X, long long xrs,
+                       long long xks, const double* Y, long long yrs, long long yks, int mode,
+                       double sign, double* Cm, long long crs, long long ccs) {
+  if (M <= 0 || N <= 0) return HQ_OK;
+  CK(hq_ozk_split(w->st, X, xrs, xks, M, K, S, 0, w->ozA, w->ozea));
+  CK(hq_ozk_split(w->st, Y, yrs, yks, N, K, S, 1, w->ozB, w->ozeb));
+  prof_mark(w, PH_SPLIT, 0.0);
+  CK(hq_ozk_gemm(w->st, &w->ds->dev, M, N, K, S, w->ozA, w->ozea, w->ozB, w->ozeb, mode, sign, Cm,
+                 crs, ccs, w->ws, w->ws_elems, w->err, spin_limit()));
+  /* flops charged: the BF16 tensor work, S(S+1)/2 digit products */
+  prof_mark(w, PH_TENSOR, (double)S * (S + 1) * M * N * (double)K);
+  return HQ_OK;
+}
+
 /* Build T for the b reflectors in U (mp rows) and apply Q^T from the left to
  * C (mp x nc2): the dlarfb('L','T','F','C') of ...var4.c:711-740. */
 static int block_reflector(hq_ws* w, int mp, int b, const double* tau, double* Cm, int ldc,
@@ -324,7 +363,17 @@ static int block_reflector(hq_ws* w, int mp, int b, const double* tau, double* C
   DG('T', 'N', b, b, mp, 1.0, w->U, w->ldu, w->U, w->ldu, 0.0, w->Z, w->ldz);
   CK(hq_larft_from_gram(w->st, b, w->Z, w->ldz, tau, w->T, w->ldt));
   prof_mark(w, PH_PANEL, 2.0 * mp * b * b + (double)b * b * b / 3.0);
-  if (nc2 > 0) {
+  if (nc2 > 0 && w->mixed) {
+    /* W1 = U^T C and C -= U W2 on the tensor cores; W2 = T^T W1 in FP64. */
+    int rc = ozk_product(w, OZK_SLICES, b, nc2, mp, w->U, w->ldu, 1, Cm, ldc, 1, 0, 1.0, w->W1,
+                         1, w->ldw);
+    if (rc) return rc;
+    DG('T', 'N', b, nc2, b, 1.0, w->T, w->ldt, w->W1, w->ldw, 0.0, w->W2, w->ldw);
+    prof_mark(w, PH_UPDATE, (double)b * b * nc2);
+    rc = ozk_product(w, OZK_SLICES, mp, nc2, b, w->U, 1, w->ldu, w->W2, w->ldw, 1, 1, -1.0, Cm, 1,
+                     ldc);
+    if (rc) return rc;
+  } else if (nc2 > 0) {
     DG('T', 'N', b, nc2, mp, 1.0, w->U, w->ldu, Cm, ldc, 0.0, w->W1, w->ldw);
     DG('T', 'N', b, nc2, b, 1.0, w->T, w->ldt, w->W1, w->ldw, 0.0, w->W2, w->ldw);
     DG('N', 'N', mp, nc2, b, -1.0, w->U, w->ldu, w->W2, w->ldw, 1.0, Cm, ldc);
@@ -347,8 +396,16 @@ static int core_hqrrp(hq_ws* w, int m, int n, double* dA, int ldda, int* djpvt, 
   /* Sketch G and Y = G A. */
   if (dG) CK(hq_copy_matrix(w->st, mY, m, dG, lddg, w->G, w->ldg));
   else CK(hq_sketch_philox(w->st, mY, m, w->G, w->ldg, seed));
-  DG('N', 'N', mY, n, m, 1.0, w->G, w->ldg, dA, ldda, 0.0, w->Y, w->ldy);
-  prof_mark(w, PH_SKETCH, 2.0 * mY * m * n);
+  if (w->mixed) {
+    /* Y^T = A^T G^T with two-digit BF16 operands: the sketch only steers pivots. */
+    prof_mark(w, PH_SKETCH, 0.0);
+    int rc = ozk_product(w, OZK_SKETCH_SLICES, n, mY, m, dA, ldda, 1, w->G, 1, w->ldg, 0, 1.0,
+                         w->Y, w->ldy, 1);
+    if (rc) return rc;
+  } else {
+    DG('N', 'N', mY, n, m, 1.0, w->G, w->ldg, dA, ldda, 0.0, w->Y, w->ldy);
+    prof_mark(w, PH_SKETCH, 2.0 * mY * m * n);
+  }
 
   for (int j = 0; j < mn; j += nb) {
     const int b = imin(nb, imin(n - j, m - j));
@@ -390,12 +447,28 @@ static int core_hqrrp(hq_ws* w, int m, int n, double* dA, int ldda, int* djpvt, 
       /* Sketch downdate (...var4.c:617-708):
        *   G_R := G_R (I - U T U^T);  Y2 -= G_R[:, 0:b] R12. */
       double* GR = w->G + (size_t)j * w->ldg;
-      DG('N', 'N', mY, b, mp, 1.0, GR, w->ldg, w->U, w->ldu, 0.0, w->Bm, w->ldb);
-      DG('N', 'N', mY, b, b, 1.0, w->Bm, w->ldb, w->T, w->ldt, 0.0, w->B2, w->ldb);
-      DG('N', 'T', mY, mp, b, -1.0, w->B2, w->ldb, w->U, w->ldu, 1.0, GR, w->ldg);
-      DG('N', 'N', mY, nc2, b, -1.0, GR, w->ldg, ABR + (size_t)b * ldda, ldda, 1.0,
-         YR + (size_t)b * w->ldy, w->ldy);
-      prof_mark(w, PH_DOWNDATE, 4.0 * mY * mp * b + 2.0 * mY * b * b + 2.0 * mY * b * nc2);
+      if (w->mixed) {
+        /* B^T = U^T G_R^T; G_R^T -= U B2^T; Y2^T -= R12^T G1^T (transposed so the
+         * long dimension is the 128-row tile side). */
+        int rc = ozk_product(w, OZK_SLICES, b, mY, mp, w->U, w->ldu, 1, GR, 1, w->ldg, 0, 1.0,
+                             w->Bm, w->ldb, 1);
+        if (rc) return rc;
+        DG('N', 'N', mY, b, b, 1.0, w->Bm, w->ldb, w->T, w->ldt, 0.0, w->B2, w->ldb);
+        prof_mark(w, PH_DOWNDATE, 2.0 * mY * b * b);
+        rc = ozk_product(w, OZK_SLICES, mp, mY, b, w->U, 1, w->ldu, w->B2, 1, w->ldb, 1, -1.0, GR,
+                         w->ldg, 1);
+        if (rc) return rc;
+        rc = ozk_product(w, OZK_SLICES, nc2, mY, b, ABR + (size_t)b * ldda, ldda, 1, GR, 1, w->ldg,
+                         1, -1.0, YR + (size_t)b * w->ldy, w->ldy, 1);
+        if (rc) return rc;
+      } else {
+        DG('N', 'N', mY, b, mp, 1.0, GR, w->ldg, w->U, w->ldu, 0.0, w->Bm, w->ldb);
+        DG('N', 'N', mY, b, b, 1.0, w->Bm, w->ldb, w->T, w->ldt, 0.0, w->B2, w->ldb);
+        DG('N', 'T', mY, mp, b, -1.0, w->B2, w->ldb, w->U, w->ldu, 1.0, GR, w->ldg);
+        DG('N', 'N', mY, nc2, b, -1.0, GR, w->ldg, ABR + (size_t)b * ldda, ldda, 1.0,
+           YR + (size_t)b * w->ldy, w->ldy);
+        prof_mark(w, PH_DOWNDATE, 4.0 * mY * mp * b + 2.0 * mY * b * b + 2.0 * mY * b * nc2);
+      }
     }
   }
   return HQ_OK;
@@ -415,6 +488,7 @@ static int ws_begin(hq_ws* w, cudaStream_t user_stream, int use_user) {
   w->ds = current_device();
   if (!w->ds) return HQ_E_CUDA;
   w->st = use_user ? user_stream : w->ds->stream;
+  w->mixed = precision() == 1;
   return HQ_OK;
 }
 
@@ -753,4 +827,50 @@ HQ_API int hqrrp_gb300_dgeqp4_device(int m, int n, double* dA, int ldda, int* d_
   CKF(cudaStreamSynchronize(st));
   free(hjp);
   return rc ? 1000 + rc : 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* FP64 GEMM on the BF16 tensor cores (split digits), device pointers.      */
+
+HQ_API int hqrrp_gb300_ozaki_dgemm(char transa, char transb, int m, int n, int k, double alpha,
+                                   const double* dA, int lda, const double* dB, int ldb,
+                                   double beta, double* dC, int ldc, int slices, void* stream) {
+  g_err[0] = 0;
+  if (m < 0 || n < 0 || k < 0 || (alpha != 1.0 && alpha != -1.0) || (beta != 0.0 && beta != 1.0) ||
+      slices < 1 || slices > 7) {
+    set_err("hqrrp_gb300_ozaki_dgemm: need m, n, k >= 0, alpha = +-1, beta in {0, 1}, "
+            "1 <= slices <= 7");
+    return HQ_E_UNSUPPORTED;
+  }
+  if (m == 0 || n == 0) return 0;
+  hq_ws w;
+  int rc = ws_begin(&w, (cudaStream_t)stream, 1);
+  if (rc) return rc;
+  const int ta = (transa == 'T' || transa == 't'), tb = (transb == 'T' || transb == 't');
+  w.ws_elems = (size_t)8 << 20;
+  w.ws = ws_alloc(&w, sizeof(double) * w.ws_elems);
+  w.ozA = ws_alloc(&w, hq_ozk_tile_bytes(m, k, slices, 0));
+  w.ozB = ws_alloc(&w, hq_ozk_tile_bytes(n, k, slices, 1));
+  w.ozea = ws_alloc(&w, sizeof(int) * (size_t)(m + 128));
+  w.ozeb = ws_alloc(&w, sizeof(int) * (size_t)(n + 128));
+  w.err = ws_alloc(&w, sizeof(int) * 2);
+  if (w.failed) rc = HQ_E_NOMEM;
+  if (!rc) {
+    int e = (int)cudaMemsetAsync(w.err, 0, sizeof(int) * 2, w.st);
+    if (e) { set_err("cudaMemsetAsync failed"); rc = HQ_E_CUDA; }
+  }
+  if (!rc && k == 0 && beta == 0.0)
+    rc = hq_dgemm(w.st, &w.ds->dev, 'N', 'N', m, n, 0, 0.0, dA, lda, dB, ldb, 0.0, dC, ldc, NULL,
+                  0) ? HQ_E_CUDA : HQ_OK;
+  else if (!rc && k > 0)
+    /* op(A) rows are the M side; op(B) columns are the N side. */
+    rc = ozk_product(&w, slices, m, n, k, dA, ta ? lda : 1, ta ? 1 : lda, dB, tb ? 1 : ldb,
+                     tb ? ldb : 1, beta == 1.0 ? 1 : 0, alpha, dC, 1, ldc);
+  if (!rc) rc = ws_check(&w);
+  ws_release(&w);
+  if (!rc) {
+    int e = (int)cudaStreamSynchronize(w.st);
+    if (e) { set_err("cudaStreamSynchronize failed: %s", cudaGetErrorString((cudaError_t)e)); rc = HQ_E_CUDA; }
+  }
+  return rc;
 }

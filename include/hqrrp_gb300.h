@@ -53,8 +53,13 @@ int NoFLA_HQRRP_WY_blk_var4(int m_A, int n_A, double* buff_A, int ldim_A, int* b
 
 /* ---- Extensions (no reference counterpart unless stated) ----------------- */
 
-/* Precision of the block updates: 0 = plain FP64 (default).  Returns the
- * previous value, or -1 for a mode this build does not provide. */
+/* Precision of the block updates: 0 = plain FP64 (default), 1 = mixed: the
+ * sketch Y = G A from two-digit BF16 operands, and the trailing update
+ * (dlarfb) and the sketch downdate as split-BF16 products on the tensor cores
+ * (seven digits per operand, exact FP32 accumulation per level, recombined in
+ * FP64); the panel, its reflectors and tau, the norm downdating, T and W2 =
+ * T^T W1 stay FP64.  HQRRP_GB300_PRECISION=mixed in the environment selects 1
+ * at first use.  Returns the previous value, or -1 for an unknown mode. */
 int hqrrp_gb300_set_precision(int mode);
 
 /* Seed of the device Philox sketch used when no sketch is supplied. */
@@ -101,11 +106,24 @@ int hqrrp_gb300_dgeqp4_device(int m, int n, double* dA, int ldda, int* d_jpvt, d
 int hqrrp_gb300_qrp_noalloc(int m, int n, double* dA, int ldda, int* d_jpvt, double* d_tau,
                             void* stream);
 
+/* C = alpha * op(A) op(B) + beta * C in FP64 emulated on the BF16 tensor
+ * cores: each operand row (of op(A)) / column (of op(B)) is scaled by a power
+ * of two and cut into `slices` 8-bit digits (6 gives about 46 correct bits
+ * relative to the row/column maxima); digit products accumulate exactly in
+ * FP32 and are recombined in FP64.  Device pointers, column-major; alpha must
+ * be +-1 and beta 0 or 1.  No counterpart in the reference: it is the
+ * product kernel of the mixed-precision path, exposed for direct use. */
+int hqrrp_gb300_ozaki_dgemm(char transa, char transb, int m, int n, int k, double alpha,
+                            const double* dA, int lda, const double* dB, int ldb, double beta,
+                            double* dC, int ldc, int slices, void* stream);
+
 /* Per-phase profiler (off by default).  While enabled, every call records
  * CUDA events at phase boundaries on its stream; read returns the summed
- * milliseconds and algorithmic FP64 flops per phase and resets them.  Phases:
- * 0 sketch + Y = G A, 1 pivot selection (sketch QRP + gathers), 2 panel QR +
- * T, 3 trailing update (dlarfb), 4 sketch downdate, 5 other.  The reference's
+ * milliseconds and flops per phase and resets them.  Phases: 0 sketch +
+ * Y = G A, 1 pivot selection (sketch QRP + gathers), 2 panel QR + T, 3
+ * trailing update (dlarfb), 4 sketch downdate, 5 other, and in mixed
+ * precision 6 the tensor-core digit products (BF16 flops) and 7 the digit
+ * splits (the FP64 parts of 3 and 4 stay in 3 and 4).  The reference's
  * libflame variant keeps the same buckets under #ifdef PROFILE
  * (libflame_sources/FLA_HQRRP_UT_blk_var2.c:165-167, :289-398).  Returns the
  * number of phases. */
