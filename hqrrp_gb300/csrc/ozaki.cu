@@ -55,13 +55,31 @@ __device__ __forceinline__ int swz64(int rr, int kk) {
   return rr * 64 + ((c ^ ((rr >> 1) & 3)) << 4) + (kk & 7) * 2;
 }
 
+// The fixed-point integer V = round(x * 2^(8S - 1 - e)) of one FP64 entry,
+// computed from its bits (no FP64 arithmetic); |V| <= 2^(8S-1).
+__device__ __forceinline__ long long fixed_point(double x, int shift_base) {
+  const long long bits = __double_as_longlong(x);
+  const int ex = (int)((bits >> 52) & 0x7FF);
+  if (ex == 0 || ex == 0x7FF) return 0;  // zeros and subnormals -> 0
+  const long long mant = (bits & 0xFFFFFFFFFFFFFLL) | (1LL << 52);
+  const int sh = ex + shift_base;
+  long long V = 0;
+  if (sh >= 0) V = mant << sh;
+  else if (sh > -63) V = (mant + (1LL << (-sh - 1))) >> (-sh);
+  return bits < 0 ? -V : V;
+}
+
 // Rows r < R of X (element (r, k) at X[r*rs + k*ks], k < K) -> S digit tiles.
-// One warp per row; rows R..RT*TR-1 and k >= K are written as zeros.
+// One warp per row; each lane takes 8-element chunks (one 16-byte group of a
+// tile row), so every digit is written with one 16-byte store.  Rows
+// R..RT*TR-1 and k >= K are written as zeros.
 __global__ void ozk_split_kernel(const double* __restrict__ X, long long rs, long long ks, int R,
                                  int K, int S, int TR, int KB, int rows_total,
                                  uint8_t* __restrict__ tiles, int* __restrict__ exps) {
   const int lane = threadIdx.x & 31;
   const int warps = blockDim.x >> 5;
+  const int nchunk = KB * (TK / 8);
+  const long long tile_bytes = (long long)TR * TK * 2;
   for (int r = blockIdx.x * warps + (threadIdx.x >> 5); r < rows_total;
        r += gridDim.x * warps) {
     const bool live = r < R;
@@ -74,29 +92,31 @@ __global__ void ozk_split_kernel(const double* __restrict__ X, long long rs, lon
     if (mx > 0.0) frexp(mx, &e);  // mx < 2^e
     if (lane == 0) exps[r] = e;
     const int rt = r / TR, rr = r % TR;
-    const int shift_base = 8 * S - 1076 - e;  // V = mant * 2^(ex + shift_base)
-    for (int k = lane; k < KB * TK; k += 32) {
-      long long V = 0;
-      if (live && k < K) {
-        const long long bits = __double_as_longlong(xr[(long long)k * ks]);
-        const int ex = (int)((bits >> 52) & 0x7FF);
-        if (ex != 0 && ex != 0x7FF) {  // zeros and subnormals -> 0
-          const long long mant = (bits & 0xFFFFFFFFFFFFFLL) | (1LL << 52);
-          const int sh = ex + shift_base;
-          if (sh >= 0) V = mant << sh;
-          else if (sh > -63) V = (mant + (1LL << (-sh - 1))) >> (-sh);
-          if (bits < 0) V = -V;
-        }
-      }
-      const int kb = k / TK, kk = k % TK;
-      uint8_t* base = tiles + ((long long)(rt * KB + kb) * S) * (TR * TK * 2) + swz64(rr, kk);
+    const int shift_base = 8 * S - 1076 - e;
+    for (int ch = lane; ch < nchunk; ch += 32) {
+      const int k0 = ch * 8;
+      long long V[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+        V[j] = (live && k0 + j < K) ? fixed_point(xr[(long long)(k0 + j) * ks], shift_base) : 0;
+      const int kb = k0 / TK, c = (k0 % TK) >> 3;
+      uint8_t* base = tiles + ((long long)(rt * KB + kb) * S) * tile_bytes + rr * 64 +
+                      ((c ^ ((rr >> 1) & 3)) << 4);
       // Balanced base-256 digits from the bottom; the top digit takes what is
       // left, which lies in [-128, 128].
       for (int s = S - 1; s >= 0; --s) {
-        const int d = s > 0 ? (int)(((V + 128) & 255) - 128) : (int)V;
-        V = (V - d) >> 8;
-        *reinterpret_cast<__nv_bfloat16*>(base + (long long)s * (TR * TK * 2)) =
-            __float2bfloat16_rn((float)d);
+        uint32_t w[4];
+#pragma unroll
+        for (int j = 0; j < 8; j += 2) {
+          const int d0 = s > 0 ? (int)(((V[j] + 128) & 255) - 128) : (int)V[j];
+          const int d1 = s > 0 ? (int)(((V[j + 1] + 128) & 255) - 128) : (int)V[j + 1];
+          V[j] = (V[j] - d0) >> 8;
+          V[j + 1] = (V[j + 1] - d1) >> 8;
+          const __nv_bfloat162 h = __floats2bfloat162_rn((float)d0, (float)d1);
+          w[j >> 1] = *reinterpret_cast<const uint32_t*>(&h);
+        }
+        *reinterpret_cast<uint4*>(base + (long long)s * tile_bytes) =
+            make_uint4(w[0], w[1], w[2], w[3]);
       }
     }
   }
@@ -357,17 +377,30 @@ __global__ void __launch_bounds__(NT, 1) ozk_gemm_kernel(OzkArgs a) {
       }
       const int r = mt * TM + warp * 32 + lane;
       if (r < a.M) {
-        const int er = a.ea[r];
-        double* crow = a.C + (long long)r * a.crs + (long long)z * a.zstride;
+        // Output in chunks of 16 columns: every load (column scales, and C in
+        // update mode) of a chunk is issued before any store, so the loads of
+        // a chunk overlap instead of each waiting behind the previous store.
+        const int* __restrict__ ebp = a.eb;
+        double* __restrict__ crow = a.C + (long long)r * a.crs + (long long)z * a.zstride;
+        const int er = a.ea[r] - 14;
 #pragma unroll
-        for (int c = 0; c < TN; ++c) {
-          const int n = nt * TN + c;
-          if (n >= a.N) continue;
-          const double v = ((double)hi[c] + (double)lo[c]);
-          const double sc = ldexp(a.sign, er + a.eb[n] - 14);
-          double* p = crow + (long long)n * a.ccs;
-          if (a.mode == 0) *p = v * sc;
-          else *p = fma(v, sc, *p);
+        for (int c0 = 0; c0 < TN; c0 += 16) {
+          int ek[16];
+          double cv[16];
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int n = nt * TN + c0 + j;
+            ek[j] = n < a.N ? er + ebp[n] : 0;
+            cv[j] = (a.mode == 1 && n < a.N) ? crow[(long long)n * a.ccs] : 0.0;
+          }
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int n = nt * TN + c0 + j;
+            if (n >= a.N) continue;
+            // hi + lo is exact in FP64; scaling by a power of two is exact.
+            const double v = ldexp(a.sign * ((double)hi[c0 + j] + (double)lo[c0 + j]), ek[j]);
+            crow[(long long)n * a.ccs] = a.mode == 0 ? v : cv[j] + v;
+          }
         }
       }
     }
