@@ -74,6 +74,16 @@ def load():
                                           C.c_double, C.c_void_p, C.c_int, C.c_void_p, C.c_int,
                                           C.c_double, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
     L.hqrrp_gb300_ozaki_dgemm.restype = C.c_int
+    L.hqrrp_gb300_qrp_batched_workspace.argtypes = [C.c_int]
+    L.hqrrp_gb300_qrp_batched_workspace.restype = C.c_size_t
+    L.hqrrp_gb300_qrp_batched_plan.argtypes = [C.c_int, _ip, _ip, C.c_void_p, C.c_size_t,
+                                               C.c_int, C.c_void_p]
+    L.hqrrp_gb300_qrp_batched_plan.restype = C.c_int
+    L.hqrrp_gb300_qrp_batched_run.argtypes = [C.c_int] + [C.c_void_p] * 7 + [C.c_int, C.c_int,
+                                                                              C.c_void_p, C.c_void_p]
+    L.hqrrp_gb300_qrp_batched_run.restype = C.c_int
+    L.hqrrp_gb300_qrp_batched_config.argtypes = [C.c_int, _ip, _ip, _ip]
+    L.hqrrp_gb300_qrp_batched_config.restype = C.c_int
     L.hqrrp_gb300_last_error.argtypes = []
     L.hqrrp_gb300_last_error.restype = C.c_char_p
     _lib = L
@@ -225,3 +235,70 @@ def ozaki_dgemm(transa, transb, alpha, At, Bt, beta, Ct, slices=6, stream=None):
                                    Ct.shape[1], int(slices), _stream_ptr(stream))
     if rc != 0:
         raise HQRRPError("ozaki_dgemm failed (%d): %s" % (rc, last_error()))
+
+
+class BatchedQRP:
+    """Pivoted QR of many small matrices in one persistent launch.
+
+    ``shapes``: list of (m, n).  ``plan`` (at construction) uploads a
+    largest-first schedule and, with ``autotune``, picks the launch shape by
+    timing.  ``run(mats)`` factors torch CUDA tensors in place -- mats[i] is
+    (n_i, m_i) contiguous, i.e. column-major A_i -- and returns (jpvt, tau,
+    info) tensors; ``run`` only enqueues work, so it can be captured in a CUDA
+    graph once the pointer tables are built (``bind``)."""
+
+    def __init__(self, shapes, autotune=True, stream=None):
+        import torch
+        L = load()
+        self.shapes = [(int(m), int(n)) for m, n in shapes]
+        self.batch = len(self.shapes)
+        self.max_n = max([n for _, n in self.shapes] + [1])
+        hm = np.array([m for m, _ in self.shapes], np.int32)
+        hn = np.array([n for _, n in self.shapes], np.int32)
+        dev = torch.device("cuda")
+        self.d_m = torch.from_numpy(hm).to(dev)
+        self.d_n = torch.from_numpy(hn).to(dev)
+        self.d_lda = torch.from_numpy(np.maximum(hm, 1)).to(dev)
+        nbytes = L.hqrrp_gb300_qrp_batched_workspace(self.batch)
+        self.work = torch.zeros(max(16, nbytes), dtype=torch.uint8, device=dev)
+        torch.cuda.synchronize()
+        cfg = L.hqrrp_gb300_qrp_batched_plan(self.batch, hm.ctypes.data_as(_ip),
+                                             hn.ctypes.data_as(_ip), self.work.data_ptr(),
+                                             self.work.numel(), 1 if autotune else 0,
+                                             _stream_ptr(stream))
+        if cfg < 0:
+            raise HQRRPError("batched plan failed (%d): %s" % (cfg, last_error()))
+        self.cfg = cfg
+        self.jpvt = [torch.zeros(n, dtype=torch.int32, device=dev) for _, n in self.shapes]
+        self.tau = [torch.zeros(max(1, min(m, n)), dtype=torch.float64, device=dev)
+                    for m, n in self.shapes]
+        self.info = torch.zeros(self.batch, dtype=torch.int32, device=dev)
+        self._ptrs = None
+
+    def config(self):
+        t, s, c = C.c_int(), C.c_int(), C.c_int()
+        load().hqrrp_gb300_qrp_batched_config(self.cfg, C.byref(t), C.byref(s), C.byref(c))
+        return {"threads": t.value, "stage_kb": s.value, "ctas_per_sm": c.value}
+
+    def bind(self, mats):
+        """Build the device pointer tables for these matrices."""
+        import torch
+        assert len(mats) == self.batch
+        for t, (m, n) in zip(mats, self.shapes):
+            assert tuple(t.shape) == (n, m) and t.is_contiguous() and t.dtype == torch.float64
+        mk = lambda xs: torch.tensor([x.data_ptr() for x in xs], dtype=torch.int64,
+                                     device="cuda")
+        self._mats = mats
+        self._ptrs = (mk(mats), mk(self.jpvt), mk(self.tau))
+
+    def run(self, mats=None, stream=None):
+        if mats is not None:
+            self.bind(mats)
+        pa, pj, pt = self._ptrs
+        rc = load().hqrrp_gb300_qrp_batched_run(
+            self.batch, self.d_m.data_ptr(), self.d_n.data_ptr(), pa.data_ptr(),
+            self.d_lda.data_ptr(), pj.data_ptr(), pt.data_ptr(), self.info.data_ptr(),
+            self.max_n, self.cfg, self.work.data_ptr(), _stream_ptr(stream))
+        if rc != 0:
+            raise HQRRPError("batched run failed (%d): %s" % (rc, last_error()))
+        return self.jpvt, self.tau, self.info

@@ -94,6 +94,15 @@ int hq_ozk_gemm(cudaStream_t stream, const hq_device_info* dev, int M, int N, in
                 double sign, double* C, long long crs, long long ccs, double* ws,
                 size_t ws_elems, int* err, unsigned spin_limit);
 
+/* ---- Batched pivoted QR (one persistent launch, device work queue) -------
+ * d_work: hq_qrp_batched_workspace(batch) bytes; ints [32..32+batch) hold the
+ * schedule (matrix indices, largest first), int 0 the queue head. */
+size_t hq_qrp_batched_workspace(int batch);
+int hq_qrp_batched(cudaStream_t stream, const hq_device_info* dev, int batch, const int* d_m,
+                   const int* d_n, double* const* d_A, const int* d_lda, int* const* d_jpvt,
+                   double* const* d_tau, int* d_info, void* d_work, int max_n, int threads,
+                   int stage_kb, int ctas_per_sm);
+
 /* ---- Launch accounting: every launcher adds the kernels it enqueued ---- */
 void hq_count_launches(int k);
 unsigned long long hq_launches(void);

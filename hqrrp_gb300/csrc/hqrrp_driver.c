@@ -874,3 +874,216 @@ HQ_API int hqrrp_gb300_ozaki_dgemm(char transa, char transb, int m, int n, int k
   }
   return rc;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Batched pivoted QR: plan (schedule + autotuned launch shape), then run.   */
+
+typedef struct {
+  int threads, stage_kb, ctas_per_sm;
+} batched_cfg;
+
+/* Launch shapes the autotuner tries: threads per CTA, shared-memory staging
+ * budget for a matrix (KB; larger matrices are worked on in place in L2),
+ * CTAs per SM. */
+static const batched_cfg g_batched_cfgs[] = {
+    {128, 0, 4},   {128, 48, 4}, {256, 0, 2},  {256, 96, 2},
+    {256, 200, 1}, {512, 96, 2}, {512, 200, 1},
+};
+#define N_BATCHED_CFGS ((int)(sizeof g_batched_cfgs / sizeof g_batched_cfgs[0]))
+
+typedef struct {
+  int batch, max_n;
+  double cost;
+  int cfg;
+} tune_entry;
+static tune_entry g_tuned[32];
+static int g_ntuned = 0;
+
+HQ_API size_t hqrrp_gb300_qrp_batched_workspace(int batch) {
+  return batch > 0 ? hq_qrp_batched_workspace(batch) : 0;
+}
+
+typedef struct {
+  double cost;
+  int idx;
+} cost_idx;
+
+static int cost_desc(const void* x, const void* y) {
+  const cost_idx *a = (const cost_idx*)x, *b = (const cost_idx*)y;
+  if (a->cost != b->cost) return a->cost < b->cost ? 1 : -1;
+  return a->idx - b->idx;
+}
+
+/* Householder QR flops (2mn^2 - 2n^3/3 for m >= n) plus one pass over A. */
+static double qr_cost(int m, int n) {
+  const double M = m > n ? m : n, k = m < n ? m : n;
+  return 2.0 * M * k * k - 2.0 * k * k * k / 3.0 + (double)m * n;
+}
+
+/* Time every launch shape on scratch matrices of the batch's sizes. */
+static int autotune_batched(hq_ws* w, int batch, const int* h_m, const int* h_n, int max_n,
+                            void* d_work) {
+  size_t total = 0;
+  for (int i = 0; i < batch; ++i) total += (size_t)(h_m[i] > 0 ? h_m[i] : 1) * (h_n[i] > 0 ? h_n[i] : 1);
+  double* pool = ws_alloc(w, sizeof(double) * total);
+  double** hA = malloc(sizeof(double*) * (size_t)batch);
+  int** hJ = malloc(sizeof(int*) * (size_t)batch);
+  double** hT = malloc(sizeof(double*) * (size_t)batch);
+  int* jbuf = ws_alloc(w, sizeof(int) * (size_t)batch * max_n);
+  double* tbuf = ws_alloc(w, sizeof(double) * (size_t)batch * max_n);
+  int* dm = ws_alloc(w, sizeof(int) * (size_t)batch);
+  int* dn = ws_alloc(w, sizeof(int) * (size_t)batch);
+  int* dl = ws_alloc(w, sizeof(int) * (size_t)batch);
+  void** dptr = ws_alloc(w, sizeof(void*) * 3 * (size_t)batch);
+  int best = -1;
+  if (!w->failed && hA && hJ && hT) {
+    size_t off = 0;
+    int* hl = malloc(sizeof(int) * (size_t)batch);
+    for (int i = 0; i < batch; ++i) {
+      hA[i] = pool + off;
+      off += (size_t)(h_m[i] > 0 ? h_m[i] : 1) * (h_n[i] > 0 ? h_n[i] : 1);
+      hJ[i] = jbuf + (size_t)i * max_n;
+      hT[i] = tbuf + (size_t)i * max_n;
+      hl[i] = h_m[i] > 1 ? h_m[i] : 1;
+    }
+    int ok = hl != NULL;
+    ok = ok && hq_sketch_philox(w->st, 1, (int)(total < 2147483647 ? total : 2147483647), pool, 1,
+                                2026ULL) == 0;
+    ok = ok && cudaMemcpyAsync(dm, h_m, sizeof(int) * batch, cudaMemcpyHostToDevice, w->st) == 0;
+    ok = ok && cudaMemcpyAsync(dn, h_n, sizeof(int) * batch, cudaMemcpyHostToDevice, w->st) == 0;
+    ok = ok && cudaMemcpyAsync(dl, hl, sizeof(int) * batch, cudaMemcpyHostToDevice, w->st) == 0;
+    ok = ok && cudaMemcpyAsync(dptr, hA, sizeof(void*) * batch, cudaMemcpyHostToDevice, w->st) == 0;
+    ok = ok && cudaMemcpyAsync(dptr + batch, hJ, sizeof(void*) * batch, cudaMemcpyHostToDevice,
+                               w->st) == 0;
+    ok = ok && cudaMemcpyAsync(dptr + 2 * batch, hT, sizeof(void*) * batch,
+                               cudaMemcpyHostToDevice, w->st) == 0;
+    ok = ok && cudaStreamSynchronize(w->st) == 0;
+    cudaEvent_t e0, e1;
+    ok = ok && cudaEventCreate(&e0) == 0 && cudaEventCreate(&e1) == 0;
+    float best_ms = 1e30f;
+    for (int c = 0; ok && c < N_BATCHED_CFGS; ++c) {
+      const batched_cfg* k = &g_batched_cfgs[c];
+      float ms = 0.f;
+      int rc = hq_qrp_batched(w->st, &w->ds->dev, batch, dm, dn, (double* const*)dptr, dl,
+                              (int* const*)(dptr + batch), (double* const*)(dptr + 2 * batch),
+                              NULL, d_work, max_n, k->threads, k->stage_kb, k->ctas_per_sm);
+      if (rc) continue; /* shape does not fit this device: skip it */
+      cudaEventRecord(e0, w->st);
+      rc = hq_qrp_batched(w->st, &w->ds->dev, batch, dm, dn, (double* const*)dptr, dl,
+                          (int* const*)(dptr + batch), (double* const*)(dptr + 2 * batch), NULL,
+                          d_work, max_n, k->threads, k->stage_kb, k->ctas_per_sm);
+      cudaEventRecord(e1, w->st);
+      if (rc || cudaStreamSynchronize(w->st) != cudaSuccess) continue;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = c;
+      }
+    }
+    if (ok) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+    }
+    free(hl);
+  }
+  free(hA);
+  free(hJ);
+  free(hT);
+  return best;
+}
+
+HQ_API int hqrrp_gb300_qrp_batched_plan(int batch, const int* h_m, const int* h_n, void* d_work,
+                                        size_t work_bytes, int autotune, void* stream) {
+  g_err[0] = 0;
+  if (batch <= 0) return 0;
+  if (work_bytes < hq_qrp_batched_workspace(batch) || !h_m || !h_n || !d_work) {
+    set_err("hqrrp_gb300_qrp_batched_plan: missing sizes or workspace too small");
+    return -HQ_E_UNSUPPORTED;
+  }
+  int max_n = 1;
+  double total = 0.0;
+  cost_idx* ord = malloc(sizeof(cost_idx) * (size_t)batch);
+  int* hord = malloc(sizeof(int) * (size_t)batch);
+  if (!ord || !hord) {
+    free(ord);
+    free(hord);
+    set_err("host allocation failed");
+    return -HQ_E_NOMEM;
+  }
+  for (int i = 0; i < batch; ++i) {
+    if (h_m[i] < 0 || h_n[i] < 0) {
+      free(ord);
+      free(hord);
+      set_err("hqrrp_gb300_qrp_batched_plan: negative size at %d", i);
+      return -HQ_E_UNSUPPORTED;
+    }
+    ord[i].cost = qr_cost(h_m[i], h_n[i]);
+    ord[i].idx = i;
+    total += ord[i].cost;
+    if (h_n[i] > max_n) max_n = h_n[i];
+  }
+  qsort(ord, (size_t)batch, sizeof(cost_idx), cost_desc);
+  for (int i = 0; i < batch; ++i) hord[i] = ord[i].idx;
+  free(ord);
+  hq_ws w;
+  int rc = ws_begin(&w, (cudaStream_t)stream, 1);
+  if (!rc) {
+    int e = (int)cudaMemcpyAsync((int*)d_work + 32, hord, sizeof(int) * batch,
+                                 cudaMemcpyHostToDevice, w.st);
+    if (!e) e = (int)cudaStreamSynchronize(w.st);
+    if (e) {
+      set_err("schedule upload failed: %s", cudaGetErrorString((cudaError_t)e));
+      rc = HQ_E_CUDA;
+    }
+  }
+  free(hord);
+  if (rc) return -rc;
+  int cfg = 3; /* 256 threads, 96 KB staging, 2 CTAs per SM */
+  if (autotune) {
+    for (int i = 0; i < g_ntuned; ++i)
+      if (g_tuned[i].batch == batch && g_tuned[i].max_n == max_n && g_tuned[i].cost == total)
+        return g_tuned[i].cfg;
+    int best = autotune_batched(&w, batch, h_m, h_n, max_n, d_work);
+    ws_release(&w);
+    cudaStreamSynchronize(w.st);
+    if (best >= 0) cfg = best;
+    if (g_ntuned < 32) {
+      g_tuned[g_ntuned].batch = batch;
+      g_tuned[g_ntuned].max_n = max_n;
+      g_tuned[g_ntuned].cost = total;
+      g_tuned[g_ntuned].cfg = cfg;
+      ++g_ntuned;
+    }
+  }
+  return cfg;
+}
+
+HQ_API int hqrrp_gb300_qrp_batched_run(int batch, const int* d_m, const int* d_n,
+                                       double* const* d_A, const int* d_lda, int* const* d_jpvt,
+                                       double* const* d_tau, int* d_info, int max_n, int cfg,
+                                       void* d_work, void* stream) {
+  g_err[0] = 0;
+  if (batch <= 0) return 0;
+  if (cfg < 0 || cfg >= N_BATCHED_CFGS || max_n <= 0) {
+    set_err("hqrrp_gb300_qrp_batched_run: bad configuration or max_n");
+    return HQ_E_UNSUPPORTED;
+  }
+  dev_state* ds = current_device();
+  if (!ds) return HQ_E_CUDA;
+  const batched_cfg* k = &g_batched_cfgs[cfg];
+  int rc = hq_qrp_batched((cudaStream_t)stream, &ds->dev, batch, d_m, d_n, d_A, d_lda, d_jpvt,
+                          d_tau, d_info, d_work, max_n, k->threads, k->stage_kb, k->ctas_per_sm);
+  if (rc) {
+    set_err("batched launch failed: %s", cudaGetErrorString((cudaError_t)rc));
+    return HQ_E_CUDA;
+  }
+  return 0;
+}
+
+HQ_API int hqrrp_gb300_qrp_batched_config(int cfg, int* threads, int* stage_kb, int* ctas_per_sm) {
+  if (cfg < 0 || cfg >= N_BATCHED_CFGS) return -1;
+  if (threads) *threads = g_batched_cfgs[cfg].threads;
+  if (stage_kb) *stage_kb = g_batched_cfgs[cfg].stage_kb;
+  if (ctas_per_sm) *ctas_per_sm = g_batched_cfgs[cfg].ctas_per_sm;
+  return N_BATCHED_CFGS;
+}

@@ -117,6 +117,30 @@ int hqrrp_gb300_ozaki_dgemm(char transa, char transb, int m, int n, int k, doubl
                             const double* dA, int lda, const double* dB, int ldb, double beta,
                             double* dC, int ldc, int slices, void* stream);
 
+/* ---- Batched small pivoted QRs (no reference counterpart as an API; the
+ * per-matrix result is that of the reference dgeqp4's small-matrix branch,
+ * LAPACK dgeqpf/dgeqp3 with all columns free: ...var4.c:189-199) ---------
+ * plan: host arrays of the batch's sizes; writes a largest-first schedule
+ * into the device workspace (hqrrp_gb300_qrp_batched_workspace bytes) and,
+ * with autotune != 0, times every launch shape on scratch matrices of these
+ * sizes once per batch signature.  Synchronous; returns the launch-shape id
+ * (>= 0) or minus an error code.
+ * run: all arrays on the device (d_A[i] column-major m[i] x n[i] with leading
+ * dimension d_lda[i], d_jpvt[i] n[i] ints, d_tau[i] min(m,n) doubles, d_info
+ * may be NULL); max_n bounds every n[i].  One persistent launch with a device
+ * work queue; asynchronous on `stream`, allocates nothing and does not
+ * synchronise, so it can be captured in a CUDA graph.  Returns 0 or an error
+ * code for the launch itself; d_info[i] != 0 flags a matrix it could not take. */
+size_t hqrrp_gb300_qrp_batched_workspace(int batch);
+int hqrrp_gb300_qrp_batched_plan(int batch, const int* h_m, const int* h_n, void* d_work,
+                                 size_t work_bytes, int autotune, void* stream);
+int hqrrp_gb300_qrp_batched_run(int batch, const int* d_m, const int* d_n, double* const* d_A,
+                                const int* d_lda, int* const* d_jpvt, double* const* d_tau,
+                                int* d_info, int max_n, int cfg, void* d_work, void* stream);
+/* Launch shape of a plan id: threads per CTA, shared-memory staging budget
+ * (KB), CTAs per SM.  Returns the number of shapes, or -1. */
+int hqrrp_gb300_qrp_batched_config(int cfg, int* threads, int* stage_kb, int* ctas_per_sm);
+
 /* Per-phase profiler (off by default).  While enabled, every call records
  * CUDA events at phase boundaries on its stream; read returns the summed
  * milliseconds and flops per phase and resets them.  Phases: 0 sketch +
