@@ -59,6 +59,7 @@ def parse():
     p.add_argument("--cpu-n", type=int, default=6144, help="CPU baseline sample size")
     p.add_argument("--ref-n", type=int, default=8192, help="reference-arm sample size")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-adjoint", action="store_true", help="skip the bwd_ms measurement")
     return p.parse_args()
 
 
@@ -309,6 +310,44 @@ def phase_table(prof):
              for k, v in prof.items()})
 
 
+def measure_adjoint(hq, device, m=4096, n=2048, k=256, nb=64, reps=5, seed=7):
+    """Forward (truncated rank-k HQRRP + Q_k R_k P^T) and backward (the
+    adjoint dL/dA of L = <W, Q_k R_k P^T>, pivots fixed) on A = U diag(i^-2) V^T
+    with Haar U (m x n orthonormal columns) and V; CUDA events, 3 warm-ups."""
+    import torch
+    g = torch.Generator(device=device).manual_seed(seed)
+
+    def orth(r, c):
+        Q, R = torch.linalg.qr(torch.randn(r, c, dtype=torch.float64, device=device, generator=g))
+        return Q * torch.sign(torch.diagonal(R))[None, :]
+
+    U, V = orth(m, n), orth(n, n)
+    sig = (1.0 + torch.arange(n, dtype=torch.float64, device=device)) ** -2.0
+    At = ((V * sig[None, :]) @ U.T).contiguous()  # column-major A (m x n)
+    Wt = torch.randn(n, m, dtype=torch.float64, device=device, generator=g)
+    del U, V
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    fwd, bwd = [], []
+    for it in range(3 + reps):
+        torch.cuda.synchronize()
+        ev[0].record()
+        Ft, jp, tau = hq.truncated_factor(At, k, nb)
+        hq.lowrank(Ft, jp, tau, k, nb)
+        ev[1].record()
+        hq.adjoint(At, Ft, jp, tau, Wt, k, nb)
+        ev[2].record()
+        torch.cuda.synchronize()
+        if it >= 3:
+            fwd.append(ev[0].elapsed_time(ev[1]))
+            bwd.append(ev[1].elapsed_time(ev[2]))
+    fwd.sort()
+    bwd.sort()
+    return {"bwd_ms": bwd[len(bwd) // 2], "fwd_ms": fwd[len(fwd) // 2],
+            "config": "m=%d n=%d k=%d nb=%d, sigma_i=i^-2, Haar U,V; median of %d after 3 "
+                      "warm-ups; fwd = truncated HQRRP + Q_k R_k P^T, bwd = adjoint "
+                      "(Q_k and T rebuilt from the reflectors)" % (m, n, k, nb, reps)}
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -404,6 +443,11 @@ def main():
                "ms_per_step": sec * 1e3, "precision": head,
                "api": "NoFLA_HQRRP_WY_blk_var4 (host pinned buffers)"}
 
+    adj = None
+    if rank == 0 and not args.no_adjoint:
+        hq.set_precision(hq.PLAIN)
+        adj = measure_adjoint(hq, device)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         kind, cores, times = cpu_oracle_run(args.cpu_n, nb, pp, 2, args.seed)
@@ -426,7 +470,8 @@ def main():
                            "l2": "inputs larger than L2 (%.1f GB matrix per step)"
                                  % (8 * m * n / 1e9)},
                 "quality": H["quality"], "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-                "gpu_launches": H["launches"], "clocks": H["clocks"], "bwd_ms": None,
+                "gpu_launches": H["launches"], "clocks": H["clocks"],
+                "bwd_ms": adj["bwd_ms"] if adj else None, "adjoint": adj,
                 "measured_peaks": {k: peaks.get(k) for k in ("hbm_gbs", "bf16_tflops",
                                                               "bf16_tflops_sustained")}}
         if "plain" in res and head != "plain":

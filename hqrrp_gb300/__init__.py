@@ -84,6 +84,21 @@ def load():
     L.hqrrp_gb300_qrp_batched_run.restype = C.c_int
     L.hqrrp_gb300_qrp_batched_config.argtypes = [C.c_int, _ip, _ip, _ip]
     L.hqrrp_gb300_qrp_batched_config.restype = C.c_int
+    L.hqrrp_gb300_hqrrp_truncated_device.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p,
+                                                      C.c_int, C.c_void_p, C.c_void_p, C.c_int,
+                                                      C.c_int, C.c_ulonglong, C.c_void_p]
+    L.hqrrp_gb300_lowrank_device.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int,
+                                             C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
+                                             C.c_void_p]
+    L.hqrrp_gb300_form_q_device.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p,
+                                            C.c_void_p, C.c_int, C.c_int, C.c_void_p]
+    L.hqrrp_gb300_hqrrp_adjoint_device.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p,
+                                                   C.c_int, C.c_void_p, C.c_int, C.c_void_p,
+                                                   C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
+                                                   C.c_int, C.c_int, C.c_void_p]
+    for f in ("hqrrp_gb300_hqrrp_truncated_device", "hqrrp_gb300_lowrank_device",
+              "hqrrp_gb300_form_q_device", "hqrrp_gb300_hqrrp_adjoint_device"):
+        getattr(L, f).restype = C.c_int
     L.hqrrp_gb300_last_error.argtypes = []
     L.hqrrp_gb300_last_error.restype = C.c_char_p
     _lib = L
@@ -302,3 +317,93 @@ class BatchedQRP:
         if rc != 0:
             raise HQRRPError("batched run failed (%d): %s" % (rc, last_error()))
         return self.jpvt, self.tau, self.info
+
+
+# ---- Truncated factorization, its low-rank reconstruction and adjoint -------
+
+def _check(rc, what):
+    if rc != 0:
+        raise HQRRPError("%s failed (%d): %s" % (what, rc, last_error()))
+
+
+def truncated_factor(At, k, nb=64, pp=10, seed=12, stream=None):
+    """Truncated HQRRP of column-major A (At: (n, m) contiguous CUDA float64).
+    Returns (Ft, jpvt, tau): Ft the factored copy, jpvt 1-based int32."""
+    import torch
+    n, m = At.shape
+    Ft = At.clone()
+    jp = torch.arange(1, n + 1, dtype=torch.int32, device=At.device)
+    tau = torch.zeros(max(1, min(m, n)), dtype=torch.float64, device=At.device)
+    _check(load().hqrrp_gb300_hqrrp_truncated_device(m, n, k, Ft.data_ptr(), m, jp.data_ptr(),
+                                                     tau.data_ptr(), nb, pp, int(seed),
+                                                     _stream_ptr(stream)), "truncated HQRRP")
+    return Ft, jp, tau
+
+
+def lowrank(Ft, jpvt, tau, k, nb=64, stream=None):
+    """Q_k R_k P^T (returned transposed: (n, m) contiguous = column-major)."""
+    import torch
+    n, m = Ft.shape
+    Out = torch.empty_like(Ft)
+    _check(load().hqrrp_gb300_lowrank_device(m, n, k, Ft.data_ptr(), m, jpvt.data_ptr(),
+                                             tau.data_ptr(), Out.data_ptr(), m, nb,
+                                             _stream_ptr(stream)), "lowrank")
+    return Out
+
+
+def form_q(Ft, tau, k, nb=64, stream=None):
+    """First k columns of Q ((k, m) contiguous = column-major m x k)."""
+    import torch
+    n, m = Ft.shape
+    Qt = torch.empty((k, m), dtype=torch.float64, device=Ft.device)
+    _check(load().hqrrp_gb300_form_q_device(m, k, Ft.data_ptr(), m, tau.data_ptr(),
+                                            Qt.data_ptr(), m, nb, _stream_ptr(stream)), "form_q")
+    return Qt
+
+
+def adjoint(At, Ft, jpvt, tau, Wt, k, nb=64, stream=None):
+    """dL/dA for L = <W, Q_k R_k P^T>, pivots fixed (all (n, m) column-major)."""
+    import torch
+    n, m = At.shape
+    Gt = torch.empty_like(At)
+    _check(load().hqrrp_gb300_hqrrp_adjoint_device(
+        m, n, k, At.data_ptr(), m, Ft.data_ptr(), m, jpvt.data_ptr(), tau.data_ptr(),
+        Wt.data_ptr(), m, Gt.data_ptr(), m, nb, _stream_ptr(stream)), "adjoint")
+    return Gt
+
+
+def _autograd_function():
+    import torch
+
+    class TruncatedHQRRP(torch.autograd.Function):
+        """A (m x n, CUDA float64) -> Q_k R_k P^T, the rank-k HQRRP
+        approximation.  Backward: the library's adjoint with the forward's
+        pivots held fixed; only A and the factored matrix (reflectors in its
+        lower part) are kept, Q and the T factors are recomputed."""
+
+        @staticmethod
+        def forward(ctx, A, k, nb=64, pp=10, seed=12):
+            At = A.detach().t().contiguous()
+            Ft, jp, tau = truncated_factor(At, k, nb, pp, seed)
+            ctx.save_for_backward(At, Ft, jp, tau)
+            ctx.k, ctx.nb = k, nb
+            return lowrank(Ft, jp, tau, k, nb).t()
+
+        @staticmethod
+        def backward(ctx, grad):
+            At, Ft, jp, tau = ctx.saved_tensors
+            Gt = adjoint(At, Ft, jp, tau, grad.t().contiguous(), ctx.k, ctx.nb)
+            return Gt.t(), None, None, None, None
+
+    return TruncatedHQRRP
+
+
+_TRUNC = None
+
+
+def truncated_hqrrp(A, k, nb=64, pp=10, seed=12):
+    """Differentiable rank-k HQRRP approximation Q_k R_k P^T of A."""
+    global _TRUNC
+    if _TRUNC is None:
+        _TRUNC = _autograd_function()
+    return _TRUNC.apply(A, k, nb, pp, seed)

@@ -1,0 +1,145 @@
+// adjoint.cu -- small kernels of the hand-written adjoint of the truncated
+// factorization A P ~= Q_k R_k (no counterpart in the reference).
+//
+// For L = <W, Q_k R_k P^T> = <W, Q Q^T A> with the pivots P held fixed, Q
+// depends only on A1 = A P[:, :k] = Q R11 (a thin Householder QR), and
+//     dL/dA = Q (Q^T W) + scatter_P( (G + Q copyltu(-G^T Q)) R11^-T ),
+//     G = W M^T + A N^T,  M = Q^T A = R_k P^T,  N = Q^T W,
+// the standard reverse-mode rule of the thin QR (copyltu(X) = tril(X) +
+// tril(X, -1)^T).  The GEMMs run on the library's product kernels; these are
+// the element-wise and triangular pieces around them.
+#include "hq_common.cuh"
+
+namespace {
+
+// U (rows x b, ldu) = unit-lower part of the reflector block stored in F.
+__global__ void unit_lower_kernel(int rows, int b, const double* __restrict__ F, int ldf,
+                                  double* __restrict__ U, int ldu) {
+  const long long total = (long long)rows * b;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e % rows), k = (int)(e / rows);
+    U[i + (long long)k * ldu] = i > k ? F[i + (long long)k * ldf] : (i == k ? 1.0 : 0.0);
+  }
+}
+
+// E (rows x k) = [I_k; 0].
+__global__ void eye_kernel(int rows, int k, double* __restrict__ E, int lde) {
+  const long long total = (long long)rows * k;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e % rows), c = (int)(e / rows);
+    E[i + (long long)c * lde] = i == c ? 1.0 : 0.0;
+  }
+}
+
+// X (k x k) <- copyltu(X) * sign: lower triangle kept, mirrored to the upper.
+__global__ void copyltu_kernel(int k, double* __restrict__ X, int ldx, double sign) {
+  const int total = k * k;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+    const int i = e % k, j = e / k;
+    if (i < j) continue;  // each thread owns a lower entry and its mirror
+    const double v = sign * X[i + (long long)j * ldx];
+    X[i + (long long)j * ldx] = v;
+    if (i != j) X[j + (long long)i * ldx] = v;
+  }
+}
+
+// Y (rows x k) <- Y R^-T for R upper triangular k x k (ldr): row-wise back
+// substitution, Y[:, j] = (Y[:, j] - sum_{i>j} Y[:, i] R[j, i]) / R[j, j].
+// One thread per row of Y; all threads of a warp read the same entry of R
+// at the same time, so R is served from L1 as a broadcast.
+__global__ void trsm_rt_kernel(int rows, int k, const double* __restrict__ R, int ldr,
+                               double* __restrict__ Y, int ldy) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
+    double* y = Y + r;
+    for (int j = k - 1; j >= 0; --j) {
+      double v = y[(long long)j * ldy];
+      for (int i = j + 1; i < k; ++i) v = fma(-y[(long long)i * ldy], __ldg(R + j + (long long)i * ldr), v);
+      y[(long long)j * ldy] = v / __ldg(R + j + (long long)j * ldr);
+    }
+  }
+}
+
+// Columns: dst[:, labels[c] - 1] (+)= src[:, c] for c < ncols (1-based labels).
+__global__ void scatter_cols_kernel(int rows, int ncols, const double* __restrict__ src, int lds,
+                                    const int* __restrict__ labels, double* __restrict__ dst,
+                                    int ldd, int accumulate) {
+  const long long total = (long long)rows * ncols;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e % rows), c = (int)(e / rows);
+    const int t = labels[c] - 1;
+    double* p = dst + i + (long long)t * ldd;
+    *p = accumulate ? *p + src[i + (long long)c * lds] : src[i + (long long)c * lds];
+  }
+}
+
+// M (k x n) = triu(F[0:k, :]) with its columns moved to their original
+// positions: M[:, labels[c] - 1] = triu part of column c.
+__global__ void rk_unpermute_kernel(int k, int n, const double* __restrict__ F, int ldf,
+                                    const int* __restrict__ labels, double* __restrict__ M,
+                                    int ldm) {
+  const long long total = (long long)k * n;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e % k), c = (int)(e / k);
+    M[i + (long long)(labels[c] - 1) * ldm] = i <= c ? F[i + (long long)c * ldf] : 0.0;
+  }
+}
+
+inline unsigned grid_for(long long total) {
+  long long b = (total + 255) / 256;
+  if (b > 8192) b = 8192;
+  return b < 1 ? 1u : (unsigned)b;
+}
+
+}  // namespace
+
+extern "C" int hq_unit_lower(cudaStream_t st, int rows, int b, const double* F, int ldf, double* U,
+                             int ldu) {
+  if (rows <= 0 || b <= 0) return 0;
+  unit_lower_kernel<<<grid_for((long long)rows * b), 256, 0, st>>>(rows, b, F, ldf, U, ldu);
+  hq_count_launches(1);
+  return (int)cudaGetLastError();
+}
+
+extern "C" int hq_eye(cudaStream_t st, int rows, int k, double* E, int lde) {
+  if (rows <= 0 || k <= 0) return 0;
+  eye_kernel<<<grid_for((long long)rows * k), 256, 0, st>>>(rows, k, E, lde);
+  hq_count_launches(1);
+  return (int)cudaGetLastError();
+}
+
+extern "C" int hq_copyltu(cudaStream_t st, int k, double* X, int ldx, double sign) {
+  if (k <= 0) return 0;
+  copyltu_kernel<<<grid_for((long long)k * k), 256, 0, st>>>(k, X, ldx, sign);
+  hq_count_launches(1);
+  return (int)cudaGetLastError();
+}
+
+extern "C" int hq_trsm_rt(cudaStream_t st, int rows, int k, const double* R, int ldr, double* Y,
+                          int ldy) {
+  if (rows <= 0 || k <= 0) return 0;
+  const unsigned blocks = (unsigned)((rows + 63) / 64);
+  trsm_rt_kernel<<<blocks, 64, 0, st>>>(rows, k, R, ldr, Y, ldy);
+  hq_count_launches(1);
+  return (int)cudaGetLastError();
+}
+
+extern "C" int hq_scatter_cols(cudaStream_t st, int rows, int ncols, const double* src, int lds,
+                               const int* labels, double* dst, int ldd, int accumulate) {
+  if (rows <= 0 || ncols <= 0) return 0;
+  scatter_cols_kernel<<<grid_for((long long)rows * ncols), 256, 0, st>>>(
+      rows, ncols, src, lds, labels, dst, ldd, accumulate);
+  hq_count_launches(1);
+  return (int)cudaGetLastError();
+}
+
+extern "C" int hq_rk_unpermute(cudaStream_t st, int k, int n, const double* F, int ldf,
+                               const int* labels, double* M, int ldm) {
+  if (k <= 0 || n <= 0) return 0;
+  rk_unpermute_kernel<<<grid_for((long long)k * n), 256, 0, st>>>(k, n, F, ldf, labels, M, ldm);
+  hq_count_launches(1);
+  return (int)cudaGetLastError();
+}

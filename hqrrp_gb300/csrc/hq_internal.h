@@ -103,6 +103,16 @@ int hq_qrp_batched(cudaStream_t stream, const hq_device_info* dev, int batch, co
                    double* const* d_tau, int* d_info, void* d_work, int max_n, int threads,
                    int stage_kb, int ctas_per_sm);
 
+/* ---- Adjoint helpers (adjoint.cu) ---- */
+int hq_unit_lower(cudaStream_t st, int rows, int b, const double* F, int ldf, double* U, int ldu);
+int hq_eye(cudaStream_t st, int rows, int k, double* E, int lde);
+int hq_copyltu(cudaStream_t st, int k, double* X, int ldx, double sign);
+int hq_trsm_rt(cudaStream_t st, int rows, int k, const double* R, int ldr, double* Y, int ldy);
+int hq_scatter_cols(cudaStream_t st, int rows, int ncols, const double* src, int lds,
+                    const int* labels, double* dst, int ldd, int accumulate);
+int hq_rk_unpermute(cudaStream_t st, int k, int n, const double* F, int ldf, const int* labels,
+                    double* M, int ldm);
+
 /* ---- Launch accounting: every launcher adds the kernels it enqueued ---- */
 void hq_count_launches(int k);
 unsigned long long hq_launches(void);

@@ -385,11 +385,14 @@ static int block_reflector(hq_ws* w, int mp, int b, const double* tau, double* C
 /* ------------------------------------------------------------------------ */
 /* HQRRP block loop (...var4.c:403-558) on device data.                      */
 
-static int core_hqrrp(hq_ws* w, int m, int n, double* dA, int ldda, int* djpvt, double* dtau,
-                      int nb, int pp, int panel_piv, const double* dG, int lddg,
-                      unsigned long long seed) {
+/* kmax < min(m, n) stops after the first kmax columns (the truncated
+ * factorization: R's first kmax rows and their reflectors); the last block
+ * then skips the sketch downdate nothing would read. */
+static int core_hqrrp_k(hq_ws* w, int m, int n, double* dA, int ldda, int* djpvt, double* dtau,
+                        int nb, int pp, int panel_piv, const double* dG, int lddg,
+                        unsigned long long seed, int kmax) {
   const hq_device_info* dev = &w->ds->dev;
-  const int mY = nb + pp, mn = imin(m, n);
+  const int mY = nb + pp, mn = imin(imin(m, n), kmax);
   const unsigned spin = spin_limit();
   if (mn == 0) return HQ_OK;
 
@@ -408,8 +411,9 @@ static int core_hqrrp(hq_ws* w, int m, int n, double* dA, int ldda, int* djpvt, 
   }
 
   for (int j = 0; j < mn; j += nb) {
-    const int b = imin(nb, imin(n - j, m - j));
+    const int b = imin(imin(nb, mn - j), imin(n - j, m - j));
     const int last = (j + nb >= m) || (j + nb >= n);
+    const int final_block = j + b >= mn;
     const int mp = m - j, nc2 = imax(0, n - j - b);
     double* AR = dA + (size_t)j * ldda;
     double* ABR = AR + j;
@@ -443,7 +447,7 @@ static int core_hqrrp(hq_ws* w, int m, int n, double* dA, int ldda, int* djpvt, 
     int rc = block_reflector(w, mp, b, dtau + j, ABR + (size_t)b * ldda, ldda, nc2);
     if (rc) return rc;
 
-    if (!last) {
+    if (!last && !(final_block && mn < imin(m, n))) {
       /* Sketch downdate (...var4.c:617-708):
        *   G_R := G_R (I - U T U^T);  Y2 -= G_R[:, 0:b] R12. */
       double* GR = w->G + (size_t)j * w->ldg;
@@ -472,6 +476,13 @@ static int core_hqrrp(hq_ws* w, int m, int n, double* dA, int ldda, int* djpvt, 
     }
   }
   return HQ_OK;
+}
+
+static int core_hqrrp(hq_ws* w, int m, int n, double* dA, int ldda, int* djpvt, double* dtau,
+                      int nb, int pp, int panel_piv, const double* dG, int lddg,
+                      unsigned long long seed) {
+  return core_hqrrp_k(w, m, n, dA, ldda, djpvt, dtau, nb, pp, panel_piv, dG, lddg, seed,
+                      imin(m, n));
 }
 
 static int check_hqrrp_shape(int nb, int pp) {
@@ -1086,4 +1097,175 @@ HQ_API int hqrrp_gb300_qrp_batched_config(int cfg, int* threads, int* stage_kb, 
   if (stage_kb) *stage_kb = g_batched_cfgs[cfg].stage_kb;
   if (ctas_per_sm) *ctas_per_sm = g_batched_cfgs[cfg].ctas_per_sm;
   return N_BATCHED_CFGS;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Truncated factorization and its adjoint.                                 */
+
+HQ_API int hqrrp_gb300_hqrrp_truncated_device(int m, int n, int k, double* dA, int ldda,
+                                              int* d_jpvt, double* d_tau, int nb, int pp,
+                                              unsigned long long seed, void* stream) {
+  g_err[0] = 0;
+  if (m < 0 || n < 0 || ldda < imax(1, m) || k < 0) {
+    set_err("invalid m, n, k or ldda");
+    return HQ_E_UNSUPPORTED;
+  }
+  const int kk = imin(k, imin(m, n));
+  if (kk == 0) return 0;
+  int rc = check_hqrrp_shape(nb, pp);
+  if (rc) return rc;
+  hq_ws w;
+  if ((rc = ws_begin(&w, (cudaStream_t)stream, 1))) return rc;
+  rc = ws_setup(&w, m, n, nb, pp, nb);
+  if (!rc) rc = core_hqrrp_k(&w, m, n, dA, ldda, d_jpvt, d_tau, nb, pp, 1, NULL, 0, seed, kk);
+  if (!rc) rc = ws_check(&w);
+  ws_release(&w);
+  if (!rc) {
+    int e = (int)cudaStreamSynchronize(w.st);
+    if (e) { set_err("cudaStreamSynchronize failed: %s", cudaGetErrorString((cudaError_t)e)); rc = HQ_E_CUDA; }
+  }
+  return rc;
+}
+
+/* Q_k (m x k, ldq) of the factorization stored in F: the reflector blocks of
+ * nb columns are rebuilt (U, Gram, T) from F and applied to [I_k; 0] from
+ * the last block to the first. */
+static int form_qk(hq_ws* w, int m, int k, int nb, const double* F, int ldf, const double* tau,
+                   double* Q, int ldq) {
+  const hq_device_info* dev = &w->ds->dev;
+  CK(hq_eye(w->st, m, k, Q, ldq));
+  const int nblk = (k + nb - 1) / nb;
+  for (int bi = nblk - 1; bi >= 0; --bi) {
+    const int j = bi * nb, b = imin(nb, k - j), mp = m - j;
+    CK(hq_unit_lower(w->st, mp, b, F + j + (size_t)j * ldf, ldf, w->U, w->ldu));
+    DG('T', 'N', b, b, mp, 1.0, w->U, w->ldu, w->U, w->ldu, 0.0, w->Z, w->ldz);
+    CK(hq_larft_from_gram(w->st, b, w->Z, w->ldz, tau + j, w->T, w->ldt));
+    /* Q[j:, :] = (I - U T U^T) Q[j:, :] */
+    const int nc = k;
+    DG('T', 'N', b, nc, mp, 1.0, w->U, w->ldu, Q + j, ldq, 0.0, w->W1, w->ldw);
+    DG('N', 'N', b, nc, b, 1.0, w->T, w->ldt, w->W1, w->ldw, 0.0, w->W2, w->ldw);
+    DG('N', 'N', mp, nc, b, -1.0, w->U, w->ldu, w->W2, w->ldw, 1.0, Q + j, ldq);
+  }
+  return HQ_OK;
+}
+
+HQ_API int hqrrp_gb300_hqrrp_adjoint_device(int m, int n, int k, const double* dA, int ldda,
+                                            const double* dF, int lddf, const int* d_jpvt,
+                                            const double* d_tau, const double* dW, int lddw,
+                                            double* dG, int lddg, int nb, void* stream) {
+  g_err[0] = 0;
+  if (m < 0 || n < 0 || k < 0 || k > imin(m, n) || ldda < imax(1, m) || lddf < imax(1, m) ||
+      lddw < imax(1, m) || lddg < imax(1, m) || nb < 1 || nb > HQ_MAX_MY) {
+    set_err("hqrrp_gb300_hqrrp_adjoint_device: invalid sizes (need k <= min(m, n))");
+    return HQ_E_UNSUPPORTED;
+  }
+  if (m == 0 || n == 0) return 0;
+  hq_ws w;
+  int rc = ws_begin(&w, (cudaStream_t)stream, 1);
+  if (rc) return rc;
+  const hq_device_info* dev;
+  rc = ws_setup(&w, m, imax(n, k), 0, 0, nb);
+  const int ldq = round_up(m, 32);
+  double* Q = rc ? NULL : ws_alloc(&w, sizeof(double) * (size_t)ldq * imax(k, 1));
+  double* GQ = rc ? NULL : ws_alloc(&w, sizeof(double) * (size_t)ldq * imax(k, 1));
+  double* Mk = rc ? NULL : ws_alloc(&w, sizeof(double) * (size_t)imax(k, 1) * n);
+  double* Nk = rc ? NULL : ws_alloc(&w, sizeof(double) * (size_t)imax(k, 1) * n);
+  double* Mp = rc ? NULL : ws_alloc(&w, sizeof(double) * (size_t)imax(k, 1) * imax(k, 1));
+  if (!rc && w.failed) rc = HQ_E_NOMEM;
+  if (!rc && k == 0) {
+    int e = (int)cudaMemset2DAsync(dG, sizeof(double) * lddg, 0, sizeof(double) * m, n, w.st);
+    if (e) { set_err("cudaMemset2DAsync failed"); rc = HQ_E_CUDA; }
+  }
+  if (!rc && k > 0) {
+    hq_ws* wp = &w;
+    dev = &wp->ds->dev;
+#define DGW(ta, tb, M, N, K, al, A, lda, B, ldb, be, C, ldc)                                  \
+  do {                                                                                       \
+    int e_ = hq_dgemm(wp->st, dev, ta, tb, M, N, K, al, A, lda, B, ldb, be, C, ldc, wp->ws,  \
+                      wp->ws_elems);                                                         \
+    if (e_) { set_err("hq_dgemm failed: %s", cudaGetErrorString((cudaError_t)e_)); rc = HQ_E_CUDA; } \
+  } while (0)
+    rc = form_qk(&w, m, k, nb, dF, lddf, d_tau, Q, ldq);
+    /* M = R_k P^T (k x n), N = Q^T W (k x n) */
+    if (!rc && hq_rk_unpermute(w.st, k, n, dF, lddf, d_jpvt, Mk, k)) rc = HQ_E_CUDA;
+    if (!rc) DGW('T', 'N', k, n, m, 1.0, Q, ldq, dW, lddw, 0.0, Nk, k);
+    /* G_Q = W M^T + A N^T (m x k) */
+    if (!rc) DGW('N', 'T', m, k, n, 1.0, dW, lddw, Mk, k, 0.0, GQ, ldq);
+    if (!rc) DGW('N', 'T', m, k, n, 1.0, dA, ldda, Nk, k, 1.0, GQ, ldq);
+    /* X = G_Q + Q copyltu(-G_Q^T Q) */
+    if (!rc) DGW('T', 'N', k, k, m, 1.0, GQ, ldq, Q, ldq, 0.0, Mp, k);
+    if (!rc && hq_copyltu(w.st, k, Mp, k, -1.0)) rc = HQ_E_CUDA;
+    if (!rc) DGW('N', 'N', m, k, k, 1.0, Q, ldq, Mp, k, 1.0, GQ, ldq);
+    /* Abar_1 = X R11^-T */
+    if (!rc && hq_trsm_rt(w.st, m, k, dF, lddf, GQ, ldq)) rc = HQ_E_CUDA;
+    /* dG = Q N, then dG[:, P_1] += Abar_1 */
+    if (!rc) DGW('N', 'N', m, n, k, 1.0, Q, ldq, Nk, k, 0.0, dG, lddg);
+    if (!rc && hq_scatter_cols(w.st, m, k, GQ, ldq, d_jpvt, dG, lddg, 1)) rc = HQ_E_CUDA;
+#undef DGW
+  }
+  if (!rc) rc = ws_check(&w);
+  ws_release(&w);
+  if (!rc) {
+    int e = (int)cudaStreamSynchronize(w.st);
+    if (e) { set_err("cudaStreamSynchronize failed: %s", cudaGetErrorString((cudaError_t)e)); rc = HQ_E_CUDA; }
+  }
+  return rc;
+}
+
+HQ_API int hqrrp_gb300_form_q_device(int m, int k, const double* dF, int lddf,
+                                     const double* d_tau, double* dQ, int lddq, int nb,
+                                     void* stream) {
+  g_err[0] = 0;
+  if (m < 0 || k < 0 || k > m || lddf < imax(1, m) || lddq < imax(1, m) || nb < 1 ||
+      nb > HQ_MAX_MY) {
+    set_err("hqrrp_gb300_form_q_device: invalid sizes");
+    return HQ_E_UNSUPPORTED;
+  }
+  if (m == 0 || k == 0) return 0;
+  hq_ws w;
+  int rc = ws_begin(&w, (cudaStream_t)stream, 1);
+  if (rc) return rc;
+  rc = ws_setup(&w, m, k, 0, 0, nb);
+  if (!rc) rc = form_qk(&w, m, k, nb, dF, lddf, d_tau, dQ, lddq);
+  if (!rc) rc = ws_check(&w);
+  ws_release(&w);
+  if (!rc) {
+    int e = (int)cudaStreamSynchronize(w.st);
+    if (e) { set_err("cudaStreamSynchronize failed: %s", cudaGetErrorString((cudaError_t)e)); rc = HQ_E_CUDA; }
+  }
+  return rc;
+}
+
+HQ_API int hqrrp_gb300_lowrank_device(int m, int n, int k, const double* dF, int lddf,
+                                      const int* d_jpvt, const double* d_tau, double* dOut,
+                                      int lddo, int nb, void* stream) {
+  g_err[0] = 0;
+  if (m < 0 || n < 0 || k < 0 || k > imin(m, n) || lddf < imax(1, m) || lddo < imax(1, m) ||
+      nb < 1 || nb > HQ_MAX_MY) {
+    set_err("hqrrp_gb300_lowrank_device: invalid sizes");
+    return HQ_E_UNSUPPORTED;
+  }
+  if (m == 0 || n == 0) return 0;
+  hq_ws w;
+  int rc = ws_begin(&w, (cudaStream_t)stream, 1);
+  if (rc) return rc;
+  rc = ws_setup(&w, m, imax(n, k), 0, 0, nb);
+  const int ldq = round_up(m, 32);
+  double* Q = rc ? NULL : ws_alloc(&w, sizeof(double) * (size_t)ldq * imax(k, 1));
+  double* Mk = rc ? NULL : ws_alloc(&w, sizeof(double) * (size_t)imax(k, 1) * n);
+  if (!rc && w.failed) rc = HQ_E_NOMEM;
+  if (!rc && k > 0) rc = form_qk(&w, m, k, nb, dF, lddf, d_tau, Q, ldq);
+  if (!rc && k > 0 && hq_rk_unpermute(w.st, k, n, dF, lddf, d_jpvt, Mk, k)) rc = HQ_E_CUDA;
+  if (!rc) {
+    int e = hq_dgemm(w.st, &w.ds->dev, 'N', 'N', m, n, k, 1.0, Q, ldq, Mk, imax(k, 1), 0.0, dOut,
+                     lddo, w.ws, w.ws_elems);
+    if (e) { set_err("hq_dgemm failed: %s", cudaGetErrorString((cudaError_t)e)); rc = HQ_E_CUDA; }
+  }
+  if (!rc) rc = ws_check(&w);
+  ws_release(&w);
+  if (!rc) {
+    int e = (int)cudaStreamSynchronize(w.st);
+    if (e) { set_err("cudaStreamSynchronize failed: %s", cudaGetErrorString((cudaError_t)e)); rc = HQ_E_CUDA; }
+  }
+  return rc;
 }

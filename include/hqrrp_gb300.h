@@ -141,6 +141,29 @@ int hqrrp_gb300_qrp_batched_run(int batch, const int* d_m, const int* d_n, doubl
  * (KB), CTAs per SM.  Returns the number of shapes, or -1. */
 int hqrrp_gb300_qrp_batched_config(int cfg, int* threads, int* stage_kb, int* ctas_per_sm);
 
+/* ---- Truncated factorization and its adjoint (no reference counterpart) --
+ * truncated: HQRRP of the device matrix dA stopped after k columns (its first
+ * k pivots, rows and reflectors are those of the full run); d_jpvt must hold
+ * 1..n on entry for the other entries below.
+ * lowrank: dOut (m x n) = Q_k R_k P^T from a truncated factorization dF.
+ * form_q: dQ (m x k) = the first k columns of Q, the reflector blocks of nb
+ * columns rebuilt from dF (T recomputed per block, nothing stored).
+ * adjoint: dG = dL/dA of L = <W, Q_k R_k P^T> with the pivots held fixed
+ * (dA the original matrix, dF/d_jpvt/d_tau its truncated factorization);
+ * the reflector blocks are recomputed, not stored.  All device pointers,
+ * column-major; each returns 0 or an error code and blocks until done. */
+int hqrrp_gb300_hqrrp_truncated_device(int m, int n, int k, double* dA, int ldda, int* d_jpvt,
+                                       double* d_tau, int nb, int pp, unsigned long long seed,
+                                       void* stream);
+int hqrrp_gb300_lowrank_device(int m, int n, int k, const double* dF, int lddf, const int* d_jpvt,
+                               const double* d_tau, double* dOut, int lddo, int nb, void* stream);
+int hqrrp_gb300_form_q_device(int m, int k, const double* dF, int lddf, const double* d_tau,
+                              double* dQ, int lddq, int nb, void* stream);
+int hqrrp_gb300_hqrrp_adjoint_device(int m, int n, int k, const double* dA, int ldda,
+                                     const double* dF, int lddf, const int* d_jpvt,
+                                     const double* d_tau, const double* dW, int lddw, double* dG,
+                                     int lddg, int nb, void* stream);
+
 /* Per-phase profiler (off by default).  While enabled, every call records
  * CUDA events at phase boundaries on its stream; read returns the summed
  * milliseconds and flops per phase and resets them.  Phases: 0 sketch +
