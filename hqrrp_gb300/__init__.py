@@ -96,7 +96,11 @@ def load():
                                                    C.c_int, C.c_void_p, C.c_int, C.c_void_p,
                                                    C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
                                                    C.c_int, C.c_int, C.c_void_p]
+    L.hqrrp_gb300_apply_q_device.argtypes = [C.c_char, C.c_int, C.c_int, C.c_int, C.c_void_p,
+                                             C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
+                                             C.c_void_p]
     for f in ("hqrrp_gb300_hqrrp_truncated_device", "hqrrp_gb300_lowrank_device",
+              "hqrrp_gb300_apply_q_device",
               "hqrrp_gb300_form_q_device", "hqrrp_gb300_hqrrp_adjoint_device"):
         getattr(L, f).restype = C.c_int
     L.hqrrp_gb300_last_error.argtypes = []
@@ -284,9 +288,16 @@ class BatchedQRP:
         if cfg < 0:
             raise HQRRPError("batched plan failed (%d): %s" % (cfg, last_error()))
         self.cfg = cfg
-        self.jpvt = [torch.zeros(n, dtype=torch.int32, device=dev) for _, n in self.shapes]
-        self.tau = [torch.zeros(max(1, min(m, n)), dtype=torch.float64, device=dev)
-                    for m, n in self.shapes]
+        # Outputs: one flat buffer each (so a caller can copy them in one
+        # transfer), handed out as per-matrix views.
+        nj = [n for _, n in self.shapes]
+        nt = [max(1, min(m, n)) for m, n in self.shapes]
+        self.jpvt_flat = torch.zeros(max(1, sum(nj)), dtype=torch.int32, device=dev)
+        self.tau_flat = torch.zeros(max(1, sum(nt)), dtype=torch.float64, device=dev)
+        oj = np.concatenate([[0], np.cumsum(nj)]).astype(int)
+        ot = np.concatenate([[0], np.cumsum(nt)]).astype(int)
+        self.jpvt = [self.jpvt_flat[oj[i]:oj[i + 1]] for i in range(self.batch)]
+        self.tau = [self.tau_flat[ot[i]:ot[i + 1]] for i in range(self.batch)]
         self.info = torch.zeros(self.batch, dtype=torch.int32, device=dev)
         self._ptrs = None
 
@@ -359,6 +370,21 @@ def form_q(Ft, tau, k, nb=64, stream=None):
     _check(load().hqrrp_gb300_form_q_device(m, k, Ft.data_ptr(), m, tau.data_ptr(),
                                             Qt.data_ptr(), m, nb, _stream_ptr(stream)), "form_q")
     return Qt
+
+
+def apply_q(Ft, tau, Ct, trans="N", k=None, nb=64, stream=None):
+    """In place: C := Q C (trans 'N') or Q^T C ('T'); Ft (n, m) and Ct (nc, m)
+    contiguous = column-major; Q = product of the first k reflectors (default
+    min(m, n)) of the factorization Ft, tau."""
+    n, m = Ft.shape
+    nc = Ct.shape[0]
+    if Ct.shape[1] != m or not Ct.is_contiguous():
+        raise ValueError("Ct must be (nc, m) contiguous")
+    k = min(m, n) if k is None else k
+    _check(load().hqrrp_gb300_apply_q_device(trans.encode(), m, nc, k, Ft.data_ptr(), m,
+                                             tau.data_ptr(), Ct.data_ptr(), m, nb,
+                                             _stream_ptr(stream)), "apply_q")
+    return Ct
 
 
 def adjoint(At, Ft, jpvt, tau, Wt, k, nb=64, stream=None):

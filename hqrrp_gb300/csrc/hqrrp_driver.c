@@ -1127,26 +1127,58 @@ HQ_API int hqrrp_gb300_hqrrp_truncated_device(int m, int n, int k, double* dA, i
   return rc;
 }
 
-/* Q_k (m x k, ldq) of the factorization stored in F: the reflector blocks of
- * nb columns are rebuilt (U, Gram, T) from F and applied to [I_k; 0] from
- * the last block to the first. */
-static int form_qk(hq_ws* w, int m, int k, int nb, const double* F, int ldf, const double* tau,
-                   double* Q, int ldq) {
+/* C (m x nc, ldc) := Q C (trans 'N') or Q^T C (trans 'T'), Q = H_0 ... H_{k-1}
+ * the product of the first k reflectors stored in F.  The reflector blocks
+ * of nb columns are rebuilt (U, Gram, T) from F and applied one at a time:
+ * from the last block to the first for Q C, first to last for Q^T C. */
+static int apply_qk(hq_ws* w, char trans, int m, int nc, int k, int nb, const double* F, int ldf,
+                    const double* tau, double* C, int ldc) {
   const hq_device_info* dev = &w->ds->dev;
-  CK(hq_eye(w->st, m, k, Q, ldq));
   const int nblk = (k + nb - 1) / nb;
-  for (int bi = nblk - 1; bi >= 0; --bi) {
+  const int tr = trans == 'T' || trans == 't';
+  for (int step = 0; step < nblk; ++step) {
+    const int bi = tr ? step : nblk - 1 - step;
     const int j = bi * nb, b = imin(nb, k - j), mp = m - j;
     CK(hq_unit_lower(w->st, mp, b, F + j + (size_t)j * ldf, ldf, w->U, w->ldu));
     DG('T', 'N', b, b, mp, 1.0, w->U, w->ldu, w->U, w->ldu, 0.0, w->Z, w->ldz);
     CK(hq_larft_from_gram(w->st, b, w->Z, w->ldz, tau + j, w->T, w->ldt));
-    /* Q[j:, :] = (I - U T U^T) Q[j:, :] */
-    const int nc = k;
-    DG('T', 'N', b, nc, mp, 1.0, w->U, w->ldu, Q + j, ldq, 0.0, w->W1, w->ldw);
-    DG('N', 'N', b, nc, b, 1.0, w->T, w->ldt, w->W1, w->ldw, 0.0, w->W2, w->ldw);
-    DG('N', 'N', mp, nc, b, -1.0, w->U, w->ldu, w->W2, w->ldw, 1.0, Q + j, ldq);
+    /* C[j:, :] -= U op(T) U^T C[j:, :] */
+    DG('T', 'N', b, nc, mp, 1.0, w->U, w->ldu, C + j, ldc, 0.0, w->W1, w->ldw);
+    DG(tr ? 'T' : 'N', 'N', b, nc, b, 1.0, w->T, w->ldt, w->W1, w->ldw, 0.0, w->W2, w->ldw);
+    DG('N', 'N', mp, nc, b, -1.0, w->U, w->ldu, w->W2, w->ldw, 1.0, C + j, ldc);
   }
   return HQ_OK;
+}
+
+/* Q_k (m x k, ldq) = Q [I_k; 0]. */
+static int form_qk(hq_ws* w, int m, int k, int nb, const double* F, int ldf, const double* tau,
+                   double* Q, int ldq) {
+  CK(hq_eye(w->st, m, k, Q, ldq));
+  return apply_qk(w, 'N', m, k, k, nb, F, ldf, tau, Q, ldq);
+}
+
+HQ_API int hqrrp_gb300_apply_q_device(char trans, int m, int nc, int k, const double* dF,
+                                      int lddf, const double* d_tau, double* dC, int lddc, int nb,
+                                      void* stream) {
+  g_err[0] = 0;
+  if ((trans != 'N' && trans != 'n' && trans != 'T' && trans != 't') || m < 0 || nc < 0 ||
+      k < 0 || k > m || lddf < imax(1, m) || lddc < imax(1, m) || nb < 1 || nb > HQ_MAX_MY) {
+    set_err("hqrrp_gb300_apply_q_device: invalid arguments");
+    return HQ_E_UNSUPPORTED;
+  }
+  if (m == 0 || nc == 0 || k == 0) return 0;
+  hq_ws w;
+  int rc = ws_begin(&w, (cudaStream_t)stream, 1);
+  if (rc) return rc;
+  rc = ws_setup(&w, m, imax(nc, k), 0, 0, nb);
+  if (!rc) rc = apply_qk(&w, trans, m, nc, k, nb, dF, lddf, d_tau, dC, lddc);
+  if (!rc) rc = ws_check(&w);
+  ws_release(&w);
+  if (!rc) {
+    int e = (int)cudaStreamSynchronize(w.st);
+    if (e) { set_err("cudaStreamSynchronize failed: %s", cudaGetErrorString((cudaError_t)e)); rc = HQ_E_CUDA; }
+  }
+  return rc;
 }
 
 HQ_API int hqrrp_gb300_hqrrp_adjoint_device(int m, int n, int k, const double* dA, int ldda,

@@ -159,6 +159,11 @@ int hqrrp_gb300_lowrank_device(int m, int n, int k, const double* dF, int lddf, 
                                const double* d_tau, double* dOut, int lddo, int nb, void* stream);
 int hqrrp_gb300_form_q_device(int m, int k, const double* dF, int lddf, const double* d_tau,
                               double* dQ, int lddq, int nb, void* stream);
+/* apply_q: dC (m x nc) := Q dC (trans 'N') or Q^T dC (trans 'T'), Q the
+ * product of the first k reflectors of a factorization dF (LAPACK dormqr
+ * with side 'L'); the reflector blocks of nb columns are rebuilt from dF. */
+int hqrrp_gb300_apply_q_device(char trans, int m, int nc, int k, const double* dF, int lddf,
+                               const double* d_tau, double* dC, int lddc, int nb, void* stream);
 int hqrrp_gb300_hqrrp_adjoint_device(int m, int n, int k, const double* dA, int ldda,
                                      const double* dF, int lddf, const int* d_jpvt,
                                      const double* d_tau, const double* dW, int lddw, double* dG,
