@@ -29,6 +29,17 @@ __device__ __forceinline__ int hq_ld_volatile(const int* p) {
 // Loads that bypass L1: data written by other CTAs during this kernel.
 __device__ __forceinline__ double hq_ldcg(const double* p) { return __ldcg(p); }
 __device__ __forceinline__ int hq_ldcg(const int* p) { return __ldcg(p); }
+__device__ __forceinline__ long long hq_ldcg(const long long* p) { return __ldcg(p); }
+
+// Order key of a column norm for pivot comparisons on the integer pipe: for
+// d >= 0 the IEEE bit pattern orders like the value; NaN maps below every
+// number (it never wins a comparison).
+__device__ __forceinline__ long long hq_norm_key(double d) {
+  const long long b = __double_as_longlong(d);
+  const long long mag = b & 0x7fffffffffffffffLL;
+  if (mag > 0x7ff0000000000000LL) return -1LL;  // NaN
+  return b < 0 ? (mag == 0 ? 0LL : -1LL) : b;  // -0 is 0; a norm is never negative
+}
 
 // Bounded grid barrier.  `counter` is zeroed before the launch; barrier number
 // `epoch` (1-based) completes when the counter reaches epoch * nctas.  Returns
@@ -111,6 +122,26 @@ __device__ __forceinline__ HqReflector hq_make_reflector(double alpha, double xn
   for (int k = 0; k < knt; ++k) beta *= safmin;
   r.beta = beta;
   return r;
+}
+
+// The same reflector from alpha and q = ||x||^2 (the tail's sum of squares).
+// Away from under/overflow, beta = -sign(alpha) sqrt(alpha^2 + q) takes one
+// square root and tau and the scale are two independent divisions -- a short
+// dependency chain, which matters where FP64 latency sits on a critical path;
+// beta agrees with DLAPY2's value to an ulp.  Near the range limits it falls
+// back to the careful form above.
+__device__ __forceinline__ HqReflector hq_make_reflector_sq(double alpha, double q) {
+  if (q == 0.0) return hq_make_reflector(alpha, 0.0);
+  const double t = fma(alpha, alpha, q);
+  if (t >= 1e-280 && t <= 1e280) {
+    HqReflector r;
+    const double beta = -copysign(sqrt(t), alpha);
+    r.tau = (beta - alpha) / beta;
+    r.scale = 1.0 / (alpha - beta);
+    r.beta = beta;
+    return r;
+  }
+  return hq_make_reflector(alpha, sqrt(q));
 }
 
 // LAPACK's tol3z = sqrt(dlamch('Epsilon')) with eps = 2^-53.

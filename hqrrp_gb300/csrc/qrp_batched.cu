@@ -140,7 +140,7 @@ __global__ void __launch_bounds__(NT) qrp_batched_kernel(BatchArgs a) {
         if (tid == 0) {
           double t = 0.0;
           for (int w = 0; w < NW; ++w) t += s_red[w];
-          const HqReflector h = hq_make_reflector(xs[s], m - s > 1 ? sqrt(t) : 0.0);
+          const HqReflector h = hq_make_reflector_sq(xs[s], m - s > 1 ? t : 0.0);
           s_tau = h.tau;
           s_scale = h.scale;
           s_beta = h.beta;

@@ -15,19 +15,28 @@
 // (one CTA per SM), kept in shared memory when they fit (108 rows x 128
 // columns = 110 KB at m = 16384) and otherwise worked on in place in L2.
 // Column swaps are then local to every CTA.  Each stage needs one grid
-// barrier: every CTA publishes, for its slab, the dot products of the pivot
+// exchange: every CTA publishes, for its slab, the dot products of the pivot
 // column with all not-yet-factored columns (the first of which is the pivot
 // column's squared norm); the owner of the pivot row also publishes that row.
-// After the barrier all CTAs hold the same reduced values (summed in a fixed
-// order, so results are reproducible) and apply the reflector to their slab
-// without further communication.  The rare norm recomputation costs one more
-// barrier in the stages that need it.
+// FP64 issue is the scarce resource on this GPU, so the sums are not formed
+// redundantly in every CTA: after a barrier, CTA c sums column c's partials
+// (laid out contiguously, one coalesced load per lane), the CTA of column 0
+// also builds the reflector, and after a second barrier every CTA loads the
+// sums, the reflector and the pivot row together.  The sums are taken in a
+// fixed order, so results are reproducible.  The slab is then updated without
+// further communication.  The norm downdate of the trailing columns carries
+// the warp-level argmax of the next pivot.
+// The rare norm recomputation costs one more barrier in the stages that need
+// it.
 #include "hq_common.cuh"
 
 namespace {
 
 constexpr int NT = 256;
 constexpr int NWARP = NT / 32;
+constexpr int MAX_G = 160;          // CTAs (one per SM); partial loads per lane <= 5
+constexpr int CB = (MAX_G + 31) / 32;
+constexpr int QB = 8;               // columns reduced per warp per batch of loads
 
 struct PnArgs {
   int mp, nc, ns, pivoting;
@@ -37,7 +46,8 @@ struct PnArgs {
   double* U;
   int ldu;
   int* perm;
-  double* part;  // [2][grid][pstride]
+  double* part;  // [2][pstride][grid] partials (column q's contiguous), then
+                 // [2][pstride + 8] reduced sums with tau, scale, beta after them
   int pstride;
   double* rowbuf;  // [2][nc]
   unsigned* bar;
@@ -45,6 +55,12 @@ struct PnArgs {
   unsigned spin_limit;
   int smem_mode, rloc_max, ldxs;
 };
+
+// Candidate order for the pivot: larger norm, then lower column (idamax's
+// first maximum); NaN never wins.
+__device__ __forceinline__ void pick(long long key, int k, long long& bkey, int& bk) {
+  if (key > bkey || (key == bkey && k < bk)) { bkey = key; bk = k; }
+}
 
 __global__ void __launch_bounds__(NT, 1) panel_qrp_kernel(PnArgs a) {
   extern __shared__ __align__(16) double smem[];
@@ -58,15 +74,14 @@ __global__ void __launch_bounds__(NT, 1) panel_qrp_kernel(PnArgs a) {
   double* sX = smem;
   double* sd = sX + (a.smem_mode ? (size_t)a.ldxs * nc : 0);
   double* se = sd + nc;
-  double* sw = se + nc;    // reduced dots, then w_k = tau * v^T X[:, k]
-  double* snew = sw + nc;  // new pivot-row entries
-  double* sred = snew + nc;  // NT scratch
-  int* sperm = (int*)(sred + NT);
+  double* sw = se + nc;      // reduced dots of the stage
+  double* srow = sw + nc;    // pivot row of the stage (old values)
+  int* sperm = (int*)(srow + nc);
   int* sflag = sperm + nc;
-  __shared__ int s_flag, s_any;
-  __shared__ double s_tau, s_scale, s_beta;
-  __shared__ double s_bd[NWARP];
+  __shared__ int s_flag;
+  __shared__ long long s_bd[NWARP];
   __shared__ int s_bk[NWARP];
+  __shared__ double s_tau, s_scale, s_beta;
 
   double* X;
   int ldx;
@@ -79,7 +94,10 @@ __global__ void __launch_bounds__(NT, 1) panel_qrp_kernel(PnArgs a) {
     X = a.P + r_lo;
     ldx = a.ldp;
   }
-  for (int k = tid; k < nc; k += NT) sperm[k] = k;
+  for (int k = tid; k < nc; k += NT) {
+    sperm[k] = k;
+    sflag[k] = 0;
+  }
   // A valid permutation is in place before any wait: if a barrier gives up
   // and the kernel returns early, the gathers that follow still read indices
   // within range.
@@ -88,84 +106,37 @@ __global__ void __launch_bounds__(NT, 1) panel_qrp_kernel(PnArgs a) {
   __syncthreads();
 
   unsigned epoch = 0;
-  auto part_w = [&](unsigned e) { return a.part + ((size_t)(e & 1) * G + cta) * a.pstride; };
-  auto part_r = [&](unsigned e) { return a.part + (size_t)(e & 1) * G * a.pstride; };
-
-  // Work split for na columns over NT threads: below NT columns, `groups`
-  // threads share a column (each takes every groups-th item of the other
-  // dimension) and their sums are combined in sred in a fixed order; from NT
-  // columns up, each thread owns columns tid, tid + NT, ...
-
-  // Sum over CTAs of the published values [0, na) into sw[0..na), in a
-  // fixed order.  Loads are issued in batches of RB independent L2 reads per
-  // thread so the reduction costs a few L2 round trips, not one per CTA.
-  constexpr int RB = 32;
-  auto reduce_parts = [&](unsigned e, int na) {
-    const double* base = part_r(e);
-    const int groups = na >= NT ? 1 : NT / na;
-    for (int q0 = 0; q0 < na; q0 += NT) {
-      const int q = q0 + tid % min(na, NT), g = tid / min(na, NT);
-      double t = 0.0;
-      if (g < groups && q < na) {
-        for (int c0 = g; c0 < G; c0 += groups * RB) {
-          double v[RB];
-#pragma unroll
-          for (int u = 0; u < RB; ++u) {
-            const int c = c0 + u * groups;
-            v[u] = c < G ? hq_ldcg(base + (size_t)c * a.pstride + q) : 0.0;
-          }
-#pragma unroll
-          for (int u = 0; u < RB; ++u) t += v[u];
-        }
-      }
-      if (groups == 1) {
-        if (g == 0 && q < na) sw[q] = t;
-      } else {
-        sred[tid] = t;
-        __syncthreads();
-        if (tid < na) {
-          double u = 0.0;
-          for (int gg = 0; gg < groups; ++gg) u += sred[gg * na + tid];
-          sw[tid] = u;
-        }
-      }
-      __syncthreads();
-    }
+  auto part_w = [&](unsigned e) { return a.part + (size_t)(e & 1) * a.pstride * G + cta; };
+  auto part_r = [&](unsigned e) { return a.part + (size_t)(e & 1) * a.pstride * G; };
+  // The pivot row of stage s goes to buffer s & 1: it is read after the
+  // stage's second barrier, and the next write to the same buffer (stage
+  // s + 2) comes after a barrier every reader has passed.
+  auto rowbuf = [&](int s) { return a.rowbuf + (size_t)(s & 1) * nc; };
+  auto red_buf = [&](unsigned e) {
+    return a.part + (size_t)2 * a.pstride * G + (size_t)(e & 1) * (a.pstride + 8);
   };
 
   // Slab-local sums over rows with global index > lo_row of x_i * X[i, k]
   // (x = column xs, or column k itself when xs < 0) for k in [k0, nc),
-  // skipping columns without sflag when use_mask; written to out[k - k0].
+  // skipping columns without sflag when use_mask; column k's sum goes to
+  // out[(k - k0) * G].  Below NT columns, `groups` adjacent lanes share a
+  // column and combine by shuffles.
   auto slab_dots = [&](int xs, int k0, int lo_row, bool use_mask, double* out) {
     const int na = nc - k0;
     const int i0 = max(0, lo_row + 1 - r_lo);
-    if (na >= NT) {
-      for (int q = tid; q < na; q += NT) {
-        const int k = k0 + q;
-        double t = 0.0;
-        if (!use_mask || sflag[k]) {
-          const double* xk = X + (size_t)k * ldx;
-          const double* xx = xs >= 0 ? X + (size_t)xs * ldx : xk;
-          double t1 = 0.0;
-          int i = i0;
-          for (; i + 1 < nloc; i += 2) {
-            t = fma(xx[i], xk[i], t);
-            t1 = fma(xx[i + 1], xk[i + 1], t1);
-          }
-          if (i < nloc) t = fma(xx[i], xk[i], t);
-          t += t1;
-        }
-        out[q] = t;
-      }
-      __syncthreads();
-      return;
+    int groups = 1;
+    if (na < NT) {
+      groups = NT / na;
+      groups = groups >= 32 ? 32 : (groups >= 16 ? 16 : (groups >= 8 ? 8 : (groups >= 4 ? 4 : (groups >= 2 ? 2 : 1))));
     }
-    const int groups = NT / na;
-    const int q = tid % na, g = tid / na;
-    double t = 0.0;
-    if (g < groups) {
+    const int g = tid % groups, stride = NT / groups;
+    // The trip count is the same for every thread, so whole warps take part
+    // in the shuffles; columns past the end contribute zero.
+    for (int q0 = 0; q0 < na; q0 += stride) {
+      const int q = q0 + tid / groups;
       const int k = k0 + q;
-      if (!use_mask || sflag[k]) {
+      double t = 0.0;
+      if (q < na && (!use_mask || sflag[k])) {
         const double* xk = X + (size_t)k * ldx;
         const double* xx = xs >= 0 ? X + (size_t)xs * ldx : xk;
         double t1 = 0.0;
@@ -177,15 +148,107 @@ __global__ void __launch_bounds__(NT, 1) panel_qrp_kernel(PnArgs a) {
         if (i < nloc) t = fma(xx[i], xk[i], t);
         t += t1;
       }
+      for (int o = groups >> 1; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+      if (g == 0 && q < na) out[(size_t)q * G] = t;
     }
-    sred[tid] = t;
-    __syncthreads();
-    if (tid < na) {
-      double u = 0.0;
-      for (int gg = 0; gg < groups; ++gg) u += sred[gg * na + tid];
-      out[tid] = u;
+  };
+
+  // sw[q] = sum over CTAs of the published column q (q < na), in a fixed
+  // order, formed in every CTA (used for the one-off initial norms and the
+  // rare norm recomputations).  Warp w takes columns w*QB.. in batches of QB,
+  // lane l the CTAs l, l+32, ...; every load of a batch is issued before any
+  // is used.
+  auto reduce_parts = [&](unsigned e, int na) {
+    const double* base = part_r(e);
+    for (int q0 = warp * QB; q0 < na; q0 += NWARP * QB) {
+      double v[QB][CB];
+#pragma unroll
+      for (int u = 0; u < QB; ++u) {
+        const int q = q0 + u;
+#pragma unroll
+        for (int j = 0; j < CB; ++j) {
+          const int c = lane + 32 * j;
+          v[u][j] = (q < na && c < G) ? hq_ldcg(base + (size_t)q * G + c) : 0.0;
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < QB; ++u) {
+        double t = v[u][0];
+#pragma unroll
+        for (int j = 1; j < CB; ++j) t += v[u][j];
+        t = hq_warp_sum(t);
+        if (lane == u && q0 + u < na) sw[q0 + u] = t;
+      }
     }
     __syncthreads();
+  };
+
+  // Reduce-scatter of stage s: warp w of CTA c sums columns c + (w + i*NWARP)*G
+  // (same fixed order as above) into the published sums; column 0's reducer
+  // also builds the reflector from the tail norm and the pivot-row entry.
+  auto reduce_scatter = [&](unsigned e, int na, int s) {
+    for (int q = cta + warp * G; q < na; q += NWARP * G) {
+      const double* col = part_r(e) + (size_t)q * G;
+      double v[CB];
+#pragma unroll
+      for (int j = 0; j < CB; ++j) {
+        const int c = lane + 32 * j;
+        v[j] = c < G ? hq_ldcg(col + c) : 0.0;
+      }
+      const double alpha = (q == 0 && lane == 0) ? hq_ldcg(rowbuf(s) + s) : 0.0;
+      double t = v[0];
+#pragma unroll
+      for (int j = 1; j < CB; ++j) t += v[j];
+      t = hq_warp_sum(t);
+      if (lane == 0) {
+        double* red = red_buf(e);
+        red[q] = t;
+        if (q == 0) {
+          const HqReflector h = hq_make_reflector_sq(alpha, (a.mp - s > 1) ? t : 0.0);
+          red[a.pstride] = h.tau;
+          red[a.pstride + 1] = h.scale;
+          red[a.pstride + 2] = h.beta;
+        }
+      }
+    }
+  };
+
+  // All-gather after the second barrier: sums, pivot row, reflector.
+  auto gather_sums = [&](unsigned e, int na, int s) {
+    const double* red = red_buf(e);
+    const double* rb = rowbuf(s) + s;
+    for (int q = tid; q < na; q += NT) {
+      const double t = hq_ldcg(red + q);
+      const double r = hq_ldcg(rb + q);
+      sw[q] = t;
+      srow[q] = r;
+    }
+    if (tid == 0) {
+      s_tau = hq_ldcg(red + a.pstride);
+      s_scale = hq_ldcg(red + a.pstride + 1);
+      s_beta = hq_ldcg(red + a.pstride + 2);
+    }
+    __syncthreads();
+  };
+
+  // Block argmax of (sd[k], k) over k in [k0, nc); every thread returns the
+  // same index (k0 when no column qualifies, e.g. all norms NaN).
+  auto block_argmax = [&](int k0) {
+    long long bd = -2;
+    int bk = 0x7fffffff;
+    for (int k = k0 + tid; k < nc; k += NT) pick(hq_norm_key(sd[k]), k, bd, bk);
+    for (int o = 16; o > 0; o >>= 1) {
+      const long long od = __shfl_xor_sync(0xffffffffu, bd, o);
+      const int ok = __shfl_xor_sync(0xffffffffu, bk, o);
+      pick(od, ok, bd, bk);
+    }
+    if (lane == 0) { s_bd[warp] = bd; s_bk[warp] = bk; }
+    __syncthreads();
+    bd = s_bd[0];
+    bk = s_bk[0];
+    for (int w = 1; w < NWARP; ++w) pick(s_bd[w], s_bk[w], bd, bk);
+    __syncthreads();  // s_bd is reused by the next call
+    return (bk == 0x7fffffff || bd < 0) ? k0 : bk;
   };
 
   // Initial norms over the whole panel.
@@ -198,47 +261,25 @@ __global__ void __launch_bounds__(NT, 1) panel_qrp_kernel(PnArgs a) {
     se[k] = sd[k];
   }
   __syncthreads();
+  int kp = a.pivoting ? block_argmax(0) : 0;
 
   for (int s = 0; s < a.ns; ++s) {
     const int na = nc - s;
-    // 1. Pivot: first maximum of the partial norms (idamax).
-    if (a.pivoting) {
-      double bd = -1.0;
-      int bk = 0x7fffffff;
-      for (int k = s + tid; k < nc; k += NT) {
-        const double d = sd[k];
-        if (d > bd || (d == bd && k < bk)) { bd = d; bk = k; }
+    // 1. Swap the pivot column into place (columns, labels, copied norms).
+    if (kp != s) {
+      double* c1 = X + (size_t)s * ldx;
+      double* c2 = X + (size_t)kp * ldx;
+      for (int i = tid; i < nloc; i += NT) {
+        const double t = c1[i];
+        c1[i] = c2[i];
+        c2[i] = t;
       }
-      for (int o = 16; o > 0; o >>= 1) {
-        const double od = __shfl_xor_sync(0xffffffffu, bd, o);
-        const int ok = __shfl_xor_sync(0xffffffffu, bk, o);
-        if (od > bd || (od == bd && ok < bk)) { bd = od; bk = ok; }
-      }
-      if (lane == 0) { s_bd[warp] = bd; s_bk[warp] = bk; }
-      __syncthreads();
       if (tid == 0) {
-        for (int w = 1; w < NWARP; ++w)
-          if (s_bd[w] > bd || (s_bd[w] == bd && s_bk[w] < bk)) { bd = s_bd[w]; bk = s_bk[w]; }
-        if (bk == 0x7fffffff) bk = s;  // all norms NaN: keep the column in place
-        s_any = bk;
-      }
-      __syncthreads();
-      const int kp = s_any;
-      if (kp != s) {
-        double* c1 = X + (size_t)s * ldx;
-        double* c2 = X + (size_t)kp * ldx;
-        for (int i = tid; i < nloc; i += NT) {
-          const double t = c1[i];
-          c1[i] = c2[i];
-          c2[i] = t;
-        }
-        if (tid == 0) {
-          const int t = sperm[s];
-          sperm[s] = sperm[kp];
-          sperm[kp] = t;
-          sd[kp] = sd[s];
-          se[kp] = se[s];
-        }
+        const int t = sperm[s];
+        sperm[s] = sperm[kp];
+        sperm[kp] = t;
+        sd[kp] = sd[s];
+        se[kp] = se[s];
       }
       __syncthreads();
     }
@@ -247,104 +288,119 @@ __global__ void __launch_bounds__(NT, 1) panel_qrp_kernel(PnArgs a) {
     //    owner of row s, that row.
     slab_dots(s, s, s, false, part_w(epoch + 1));
     if (s >= r_lo && s < r_hi) {
-      double* rb = a.rowbuf + (size_t)((epoch + 1) & 1) * nc;
+      double* rb = rowbuf(s);
       for (int k = s + tid; k < nc; k += NT) rb[k] = X[(s - r_lo) + (size_t)k * ldx];
     }
     ++epoch;
     if (!hq_grid_barrier(a.bar, a.err, epoch, a.spin_limit, &s_flag)) return;
 
-    // 3. Reduce; build the reflector; w_k = tau * v^T X[:, k].
-    reduce_parts(epoch, na);
-    const double* rb = a.rowbuf + (size_t)(epoch & 1) * nc;
-    if (tid == 0) {
-      const double alpha = hq_ldcg(rb + s);
-      const HqReflector h = hq_make_reflector(alpha, (a.mp - s > 1) ? sqrt(sw[0]) : 0.0);
-      s_tau = h.tau;
-      s_scale = h.scale;
-      s_beta = h.beta;
-      if (cta == 0) a.tau[s] = h.tau;
-    }
-    __syncthreads();
+    // 3. Reduce-scatter, second barrier, all-gather of the sums and of the
+    //    reflector (built once, by column 0's reducer).
+    const unsigned e_pub = epoch;
+    reduce_scatter(e_pub, na, s);
+    ++epoch;
+    if (!hq_grid_barrier(a.bar, a.err, epoch, a.spin_limit, &s_flag)) return;
+    gather_sums(e_pub, na, s);
     const double tau = s_tau, scale = s_scale;
-    // sw[k - s] (k > s) becomes w_k; snew[k] is the new pivot-row entry.
-    for (int k = s + 1 + tid; k < nc; k += NT) {
-      const double row = hq_ldcg(rb + k);
-      const double w = tau * fma(scale, sw[k - s], row);
-      sw[k - s] = w;
-      snew[k] = row - w;
+    if (cta == 0 && tid == 0) a.tau[s] = tau;
+    {
+      // v = [1; scale * x] in place (rows > s), beta on the diagonal.
+      double* xs = X + (size_t)s * ldx;
+      for (int i = max(0, s + 1 - r_lo) + tid; i < nloc; i += NT) xs[i] *= scale;
+      if (tid == 0 && s >= r_lo && s < r_hi) xs[s - r_lo] = s_beta;
     }
     __syncthreads();
-    // 4. Update the slab: X[i,k] -= (scale * x_i) * w_k for rows > s.
+
+    // 4. Update the slab: X[i,k] -= v_i * w_k for rows > s, with
+    //    w_k = tau * v^T X[:, k] = tau * (scale * dot_k + row_k); the owner of
+    //    row s stores the new row entries row_k - w_k.
     {
       const int nt = nc - s - 1;
       const int i0 = max(0, s + 1 - r_lo);
       const bool own = (s >= r_lo && s < r_hi);
-      const double* xs = X + (size_t)s * ldx;
+      const double* v = X + (size_t)s * ldx;
       if (nt >= NT) {
         for (int q = tid; q < nt; q += NT) {
           const int k = s + 1 + q;
-          const double wk = sw[q + 1];
+          const double wk = tau * fma(scale, sw[q + 1], srow[q + 1]);
           double* xk = X + (size_t)k * ldx;
-          for (int i = i0; i < nloc; ++i) xk[i] = fma(-(scale * xs[i]), wk, xk[i]);
-          if (own) xk[s - r_lo] = snew[k];
+          for (int i = i0; i < nloc; ++i) xk[i] = fma(-v[i], wk, xk[i]);
+          if (own) xk[s - r_lo] = srow[q + 1] - wk;
         }
       } else if (nt > 0) {
         const int groups = NT / nt;
         const int q = tid % nt, g = tid / nt;
         if (g < groups) {
           const int k = s + 1 + q;
-          const double wk = sw[q + 1];
+          const double wk = tau * fma(scale, sw[q + 1], srow[q + 1]);
           double* xk = X + (size_t)k * ldx;
-          for (int i = i0 + g; i < nloc; i += groups) xk[i] = fma(-(scale * xs[i]), wk, xk[i]);
-          if (own && g == 0) xk[s - r_lo] = snew[k];
+          for (int i = i0 + g; i < nloc; i += groups) xk[i] = fma(-v[i], wk, xk[i]);
+          if (own && g == 0) xk[s - r_lo] = srow[q + 1] - wk;
         }
       }
-    }
-    __syncthreads();
-    {
-      double* xs = X + (size_t)s * ldx;
-      const int i0 = max(0, s + 1 - r_lo);
-      for (int i = i0 + tid; i < nloc; i += NT) xs[i] *= scale;
-      if (tid == 0 && s >= r_lo && s < r_hi) xs[s - r_lo] = s_beta;
     }
 
-    // 5. Norm downdate; recompute flagged norms with one more barrier.
-    if (a.pivoting) {
-      int any = 0;
-      for (int k = s + 1 + tid; k < nc; k += NT) {
-        int flag = 0;
-        double dk = sd[k];
-        if (dk != 0.0) {
-          const double r = snew[k];
-          double t1 = fabs(r) / dk;
-          t1 = (1.0 + t1) * (1.0 - t1);
-          if (0.0 > t1) t1 = 0.0;
-          const double ratio = dk / se[k];
-          const double t2 = t1 * ratio * ratio;
-          if (t2 <= HQ_TOL3Z) flag = 1;
-          else sd[k] = dk * sqrt(t1);
+    // 5. Norm downdate of the trailing columns with the next pivot's warp
+    //    argmax; recompute flagged norms with one more barrier.
+    if (!a.pivoting) {
+      __syncthreads();
+      kp = s + 1;
+      continue;
+    }
+    int any = 0;
+    long long bd = -2;
+    int bk = 0x7fffffff;
+    for (int k = s + 1 + tid; k < nc; k += NT) {
+      const int q = k - s;
+      const double wk = tau * fma(scale, sw[q], srow[q]);
+      const double r = srow[q] - wk;  // the new entry of row s
+      int flag = 0;
+      double dk = sd[k];
+      if (dk != 0.0) {
+        double t1 = fabs(r) / dk;
+        t1 = (1.0 + t1) * (1.0 - t1);
+        if (0.0 > t1) t1 = 0.0;
+        const double ratio = dk / se[k];
+        const double t2 = t1 * ratio * ratio;
+        if (t2 <= HQ_TOL3Z) {
+          flag = 1;
+        } else {
+          dk *= sqrt(t1);
+          sd[k] = dk;
         }
-        sflag[k] = flag;
-        any |= flag;
       }
-      any = __syncthreads_or(any);
-      if (any) {
-        for (int k = tid; k <= s; k += NT) sflag[k] = 0;
-        __syncthreads();
-        slab_dots(-1, s, s, true, part_w(epoch + 1));
-        ++epoch;
-        if (!hq_grid_barrier(a.bar, a.err, epoch, a.spin_limit, &s_flag)) return;
-        reduce_parts(epoch, na);
-        for (int k = s + 1 + tid; k < nc; k += NT) {
-          if (sflag[k]) {
-            const double nv = (a.mp - s - 1 > 0) ? sqrt(sw[k - s]) : 0.0;
-            sd[k] = nv;
-            se[k] = nv;
-          }
-        }
+      sflag[k] = flag;
+      any |= flag;
+      pick(hq_norm_key(dk), k, bd, bk);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const long long od = __shfl_xor_sync(0xffffffffu, bd, o);
+      const int ok = __shfl_xor_sync(0xffffffffu, bk, o);
+      pick(od, ok, bd, bk);
+    }
+    if (lane == 0) { s_bd[warp] = bd; s_bk[warp] = bk; }
+    any = __syncthreads_or(any);
+    if (!any) {
+      bd = s_bd[0];
+      bk = s_bk[0];
+      for (int w = 1; w < NWARP; ++w) pick(s_bd[w], s_bk[w], bd, bk);
+      kp = (bk == 0x7fffffff || bd < 0) ? s + 1 : bk;
+      continue;  // s_bd is next written after the next stage's grid barrier
+    }
+    slab_dots(-1, s, s, true, part_w(epoch + 1));
+    ++epoch;
+    if (!hq_grid_barrier(a.bar, a.err, epoch, a.spin_limit, &s_flag)) return;
+    reduce_parts(epoch, na);
+    for (int k = s + 1 + tid; k < nc; k += NT) {
+      if (sflag[k]) {
+        const double nv = (a.mp - s - 1 > 0) ? sqrt(sw[k - s]) : 0.0;
+        sd[k] = nv;
+        se[k] = nv;
+        sflag[k] = 0;
       }
     }
     __syncthreads();
+    kp = block_argmax(s + 1);
   }
 
   // Write back, explicit unit-lower U, permutation.
@@ -366,6 +422,7 @@ __global__ void __launch_bounds__(NT, 1) panel_qrp_kernel(PnArgs a) {
 int panel_grid(const hq_device_info* dev, int mp) {
   int g = (mp + 63) / 64;
   if (g > dev->num_sms) g = dev->num_sms;
+  if (g > MAX_G) g = MAX_G;
   return g < 1 ? 1 : g;
 }
 
@@ -404,7 +461,8 @@ __global__ void larft_kernel(int k, const double* __restrict__ Z, int ldz,
 }  // namespace
 
 extern "C" size_t hq_panel_part_elems(const hq_device_info* dev, int nc) {
-  return (size_t)2 * dev->num_sms * (size_t)((nc + 2) & ~1);
+  const size_t ps = (size_t)((nc + 2) & ~1);
+  return (size_t)2 * dev->num_sms * ps + 2 * (ps + 8);
 }
 
 extern "C" int hq_panel_qrp(cudaStream_t stream, const hq_device_info* dev, int mp, int nc,
@@ -431,10 +489,11 @@ extern "C" int hq_panel_qrp(cudaStream_t stream, const hq_device_info* dev, int 
   a.err = err;
   a.spin_limit = spin_limit;
   const int G = panel_grid(dev, mp);
-  if ((size_t)2 * G * a.pstride > part_elems) return (int)cudaErrorInvalidValue;
+  if ((size_t)2 * G * a.pstride + 2 * ((size_t)a.pstride + 8) > part_elems)
+    return (int)cudaErrorInvalidValue;
   a.rloc_max = (mp + G - 1) / G;
   a.ldxs = a.rloc_max | 1;
-  const size_t fixed = sizeof(double) * (4 * (size_t)nc + NT) + sizeof(int) * (2 * (size_t)nc + 2);
+  const size_t fixed = sizeof(double) * (4 * (size_t)nc) + sizeof(int) * (2 * (size_t)nc + 2);
   const size_t with_x = fixed + sizeof(double) * (size_t)a.ldxs * nc;
   size_t smem;
   if (with_x <= dev->smem_optin) {

@@ -195,7 +195,7 @@ __global__ void __launch_bounds__(NT, 1) skinny_qrp_kernel(SkArgs a) {
       for (int r = s + 1 + lane; r < mY; r += 32) q = fma(sv[r], sv[r], q);
       q = hq_warp_sum(q);
       if (lane == 0) {
-        const HqReflector h = hq_make_reflector(sv[s], sqrt(q));
+        const HqReflector h = hq_make_reflector_sq(sv[s], q);
         s_tau = h.tau;
         sred[0] = h.scale;
       }
@@ -268,6 +268,260 @@ __global__ void __launch_bounds__(NT, 1) skinny_qrp_kernel(SkArgs a) {
   }
 }
 
+// Register-resident variant: two adjacent lanes hold one sketch column, rows
+// interleaved (lane parity h holds rows 2i + h, i < RPT), so a stage reads its
+// columns from registers instead of shared memory; the reflector is staged in
+// shared memory (zero above the stage's row, so whole chunks of 16 rows above
+// it are skipped).  FP64 issue is the scarce resource on this GPU, so scalar
+// work is done once, not by every thread: one lane builds the reflector, one
+// thread per column downdates its norm, and pivot candidates compare integer
+// keys.  Used when a CTA's range has at most NT/2 columns and mY <= 2 * RPT;
+// otherwise the shared-memory kernel above runs.  Record layout (as 64-bit
+// integers): [0] norm key, [1] position, [2] column, then the column's entries.
+__device__ __forceinline__ bool better_key(long long k1, int p1, long long k2, int p2) {
+  return k1 > k2 || (k1 == k2 && p1 < p2);
+}
+
+template <int RPT>
+__global__ void __launch_bounds__(NT, 1) skinny_qrp_reg_kernel(SkArgs a) {
+  constexpr int NCH = RPT / 8;  // chunks of 8 registers = 16 rows
+  constexpr int NC = NT / 2;
+  __shared__ __align__(16) double sv[2 * RPT];   // winner column (raw)
+  __shared__ __align__(16) double sv2[2 * RPT];  // the reflector v
+  __shared__ long long s_bk[NWARP];
+  __shared__ int s_bp[NWARP], s_bc[NWARP];
+  __shared__ int spos[NC], sflag[NC];
+  __shared__ double sd[NC], se[NC], srs[NC];
+  __shared__ int s_flag, s_win_pos, s_win_cta, s_win_col;
+  __shared__ double s_tau, s_scale;
+  const int P = gridDim.x, cta = blockIdx.x, tid = threadIdx.x;
+  const int lane = tid & 31, warp = tid >> 5, h = lane & 1;
+  const unsigned pmask = 3u << (lane & 30);
+  const int mY = a.mY;
+  const int c_lo = (int)((long long)cta * a.N / P);
+  const int c_hi = (int)((long long)(cta + 1) * a.N / P);
+  const int nloc = c_hi - c_lo;
+  const int c = tid >> 1;  // this pair's local column
+  const bool have = c < nloc;
+
+  double x[RPT];
+  {
+    const double* src = a.Y + (size_t)(c_lo + (have ? c : 0)) * a.ldy;
+    double q = 0.0;
+#pragma unroll
+    for (int i = 0; i < RPT; ++i) {
+      const int r = 2 * i + h;
+      x[i] = (have && r < mY) ? src[r] : 0.0;
+      q = fma(x[i], x[i], q);
+    }
+    q += __shfl_xor_sync(0xffffffffu, q, 1);
+    if (have && h == 0) {
+      sd[c] = sqrt(q);
+      se[c] = sd[c];
+      spos[c] = c_lo + c;
+    }
+  }
+  for (int r = tid; r < 2 * RPT; r += NT) sv2[r] = 0.0;
+  __syncthreads();
+
+  unsigned epoch = 0;
+  // Publish this CTA's best candidate for stage s (entries from row s on).
+  auto publish = [&](int s) {
+    long long bk = -2;
+    int bp = 0x7fffffff, bc = -1;
+    if (tid < nloc && spos[tid] >= s) {
+      bk = hq_norm_key(sd[tid]);
+      bp = spos[tid];
+      bc = tid;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const long long ok = __shfl_xor_sync(0xffffffffu, bk, o);
+      const int op = __shfl_xor_sync(0xffffffffu, bp, o);
+      const int oc = __shfl_xor_sync(0xffffffffu, bc, o);
+      if (better_key(ok, op, bk, bp)) { bk = ok; bp = op; bc = oc; }
+    }
+    if (lane == 0) { s_bk[warp] = bk; s_bp[warp] = bp; s_bc[warp] = bc; }
+    __syncthreads();
+    bk = s_bk[0];
+    bp = s_bp[0];
+    bc = s_bc[0];
+    for (int w = 1; w < NWARP; ++w)
+      if (better_key(s_bk[w], s_bp[w], bk, bp)) { bk = s_bk[w]; bp = s_bp[w]; bc = s_bc[w]; }
+    double* rec = a.part + ((size_t)((epoch + 1) & 1) * P + cta) * a.rec;
+    if (tid == 0) {
+      long long* hdr = reinterpret_cast<long long*>(rec);
+      hdr[0] = bk;
+      hdr[1] = bp;
+      hdr[2] = bc >= 0 ? c_lo + bc : -1;
+    }
+    if (bc >= 0 && c == bc) {
+#pragma unroll
+      for (int i = 0; i < RPT; ++i) {
+        const int r = 2 * i + h;
+        if (r >= s && r < mY) rec[HDR + r] = x[i];
+      }
+    }
+  };
+
+  publish(0);
+  for (int s = 0; s < a.b; ++s) {
+    ++epoch;
+    if (!hq_grid_barrier(a.bar, a.err, epoch, a.spin_limit, &s_flag)) return;
+    const double* recs = a.part + (size_t)(epoch & 1) * P * a.rec;
+
+    // Winner: every CTA reduces the same records in the same way; all header
+    // loads are issued before any is used.
+    if (warp == 0) {
+      constexpr int QL = 5;  // records per lane: P <= 160
+      long long kk[QL];
+      int pp[QL], cc[QL];
+#pragma unroll
+      for (int j = 0; j < QL; ++j) {
+        const int q = lane + 32 * j;
+        const long long* hdr = reinterpret_cast<const long long*>(recs + (size_t)q * a.rec);
+        kk[j] = q < P ? hq_ldcg(hdr) : -3;
+        pp[j] = q < P ? (int)hq_ldcg(hdr + 1) : 0x7fffffff;
+        cc[j] = q < P ? (int)hq_ldcg(hdr + 2) : -1;
+      }
+      long long bk = -3;
+      int bp = 0x7fffffff, bq = -1, bcol = -1;
+#pragma unroll
+      for (int j = 0; j < QL; ++j)
+        if (kk[j] > -2 && better_key(kk[j], pp[j], bk, bp)) {
+          bk = kk[j];
+          bp = pp[j];
+          bq = lane + 32 * j;
+          bcol = cc[j];
+        }
+      for (int o = 16; o > 0; o >>= 1) {
+        const long long ok = __shfl_xor_sync(0xffffffffu, bk, o);
+        const int op = __shfl_xor_sync(0xffffffffu, bp, o);
+        const int oq = __shfl_xor_sync(0xffffffffu, bq, o);
+        const int ocol = __shfl_xor_sync(0xffffffffu, bcol, o);
+        if (better_key(ok, op, bk, bp)) { bk = ok; bp = op; bq = oq; bcol = ocol; }
+      }
+      if (lane == 0) {
+        s_win_pos = bp;
+        s_win_cta = bq;
+        s_win_col = bcol;
+      }
+    }
+    __syncthreads();
+    const int wpos = s_win_pos, wcta = s_win_cta, wcol = s_win_col;
+    if (wcta < 0) {  // no active column anywhere: cannot happen for b <= N
+      if (tid == 0) atomicCAS(a.err, 0, HQ_ERR_BAD_SHAPE);
+      return;
+    }
+    // Position bookkeeping for the swap of positions s and wpos (columns are
+    // never moved).
+    if (tid < nloc) {
+      if (wpos != s && spos[tid] == s) spos[tid] = wpos;
+      if (cta == wcta && c_lo + tid == wcol) spos[tid] = s;
+    }
+    // Winner column, rows s..mY-1.
+    const double* wrec = recs + (size_t)wcta * a.rec + HDR;
+    for (int r = s + tid; r < mY; r += NT) sv[r] = hq_ldcg(wrec + r);
+    __syncthreads();
+    if (s + 1 == a.b) break;  // the pivots are complete; V is discarded
+    // Warp 0: tail norm, reflector (one lane), v = [1; scale * tail].
+    if (warp == 0) {
+      double q = 0.0;
+      for (int r = s + 1 + lane; r < mY; r += 32) q = fma(sv[r], sv[r], q);
+      q = hq_warp_sum(q);
+      if (lane == 0) {
+        const HqReflector hr = hq_make_reflector_sq(sv[s], q);
+        s_tau = hr.tau;
+        s_scale = hr.scale;
+      }
+      __syncwarp();
+      const double scale = s_scale;
+      for (int r = s + 1 + lane; r < mY; r += 32) sv2[r] = scale * sv[r];
+      if (lane == 0) {
+        sv2[s] = 1.0;
+        if (s > 0) sv2[s - 1] = 0.0;
+      }
+    }
+    __syncthreads();
+
+    // Apply H = I - tau v v^T to this pair's column (if still active); the
+    // new entry of row s goes to srs for the downdate.
+    const bool active = have && spos[c] > s;
+    if (active) {
+      const int sch = s >> 4;  // first chunk holding a row >= s
+      double w = 0.0;
+#pragma unroll
+      for (int ch = 0; ch < NCH; ++ch) {
+        if (ch >= sch && 16 * ch < mY) {
+#pragma unroll
+          for (int j = 0; j < 8; ++j) w = fma(sv2[16 * ch + 2 * j + h], x[8 * ch + j], w);
+        }
+      }
+      w += __shfl_xor_sync(pmask, w, 1);
+      const double g = -s_tau * w;
+      double xs_new = 0.0;
+#pragma unroll
+      for (int ch = 0; ch < NCH; ++ch) {
+        if (ch >= sch && 16 * ch < mY) {
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            x[8 * ch + j] = fma(g, sv2[16 * ch + 2 * j + h], x[8 * ch + j]);
+            if (16 * ch + 2 * j + h == s) xs_new = x[8 * ch + j];
+          }
+        }
+      }
+      if (h == (s & 1)) srs[c] = xs_new;
+    }
+    __syncthreads();
+    // Norm downdate, one thread per column (LAWN 176); flagged norms are
+    // recomputed from the pair's registers.
+    int flag = 0;
+    if (tid < nloc && spos[tid] > s) {
+      double dc = sd[tid];
+      if (dc != 0.0) {
+        double t1 = fabs(srs[tid]) / dc;
+        t1 = (1.0 + t1) * (1.0 - t1);
+        if (0.0 > t1) t1 = 0.0;
+        const double ratio = dc / se[tid];
+        const double t2 = t1 * ratio * ratio;
+        if (t2 <= HQ_TOL3Z) flag = 1;
+        else sd[tid] = dc * sqrt(t1);
+      }
+    }
+    if (tid < NC) sflag[tid] = flag;
+    if (__syncthreads_or(flag)) {
+      if (active && sflag[c]) {
+        double q2 = 0.0;
+#pragma unroll
+        for (int i = 0; i < RPT; ++i) {
+          const int r = 2 * i + h;
+          if (r > s) q2 = fma(x[i], x[i], q2);
+        }
+        q2 += __shfl_xor_sync(pmask, q2, 1);
+        const double dc = (mY - s - 1 > 0) ? sqrt(q2) : 0.0;
+        if (h == 0) {
+          sd[c] = dc;
+          se[c] = dc;
+        }
+      }
+      __syncthreads();
+    }
+    publish(s + 1);
+  }
+
+  // Final permutation as (dst, src) pairs for the columns that moved.
+  for (int cc = tid; cc < nloc; cc += NT) {
+    if (spos[cc] != c_lo + cc) {
+      const int i = atomicAdd(a.npairs, 1);
+      if (i < a.max_pairs) {
+        a.pairs[2 * i] = spos[cc];
+        a.pairs[2 * i + 1] = c_lo + cc;
+      } else {
+        atomicCAS(a.err, 0, HQ_ERR_BAD_SHAPE);  // only after an aborted run
+      }
+    }
+  }
+}
+
 int skinny_grid(const hq_device_info* dev, int N) {
   int p = (N + 15) / 16;
   if (p > dev->num_sms) p = dev->num_sms;
@@ -318,14 +572,23 @@ extern "C" int hq_skinny_qrp(cudaStream_t stream, const hq_device_info* dev, int
     smem = fixed;
     if (V == nullptr || smem > dev->smem_optin) return (int)cudaErrorInvalidValue;
   }
-  cudaError_t e = cudaFuncSetAttribute(skinny_qrp_kernel,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return (int)e;
+  cudaError_t e;
   if ((e = cudaMemsetAsync(bar, 0, sizeof(unsigned), stream)) != cudaSuccess) return (int)e;
   if ((e = cudaMemsetAsync(npairs, 0, sizeof(int), stream)) != cudaSuccess) return (int)e;
   void* args[] = {&a};
-  e = cudaLaunchCooperativeKernel((const void*)skinny_qrp_kernel, dim3(P), dim3(NT), args, smem,
-                                  stream);
+  const void* fn = nullptr;
+  const bool reg_ok = a.nloc_max <= NT / 2 && P <= 160;  // 5 records per lane in the winner pick
+  if (reg_ok && mY <= 2 * 40) fn = (const void*)skinny_qrp_reg_kernel<40>;
+  else if (reg_ok && mY <= 2 * 72) fn = (const void*)skinny_qrp_reg_kernel<72>;
+  if (fn != nullptr) {
+    e = cudaLaunchCooperativeKernel(fn, dim3(P), dim3(NT), args, 0, stream);
+  } else {
+    e = cudaFuncSetAttribute(skinny_qrp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+    if (e != cudaSuccess) return (int)e;
+    e = cudaLaunchCooperativeKernel((const void*)skinny_qrp_kernel, dim3(P), dim3(NT), args, smem,
+                                    stream);
+  }
   hq_count_launches(1);
   return (int)e;
 }
