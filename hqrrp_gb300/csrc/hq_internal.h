@@ -93,6 +93,13 @@ int hq_ozk_gemm(cudaStream_t stream, const hq_device_info* dev, int M, int N, in
                 const void* Atiles, const int* ea, const void* Btiles, const int* eb, int mode,
                 double sign, double* C, long long crs, long long ccs, double* ws,
                 size_t ws_elems, int* err, unsigned spin_limit);
+/* K <= 256: persistent kernel with double-buffered TMEM; the N side must be
+ * split with side 2 (32-row tiles). */
+int hq_ozk_short_ok(int K);
+int hq_ozk_gemm_short(cudaStream_t stream, const hq_device_info* dev, int M, int N, int K, int S,
+                      const void* Atiles, const int* ea, const void* Btiles, const int* eb,
+                      int mode, double sign, double* C, long long crs, long long ccs, int* err,
+                      unsigned spin_limit);
 
 /* ---- Batched pivoted QR (one persistent launch, device work queue) -------
  * d_work: hq_qrp_batched_workspace(batch) bytes; ints [32..32+batch) hold the

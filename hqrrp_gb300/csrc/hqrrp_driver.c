@@ -345,11 +345,16 @@ static int ozk_product(hq_ws* w, int S, int M, int N, int K, const double* X, lo
                        long long xks, const double* Y, long long yrs, long long yks, int mode,
                        double sign, double* Cm, long long crs, long long ccs) {
   if (M <= 0 || N <= 0) return HQ_OK;
+  const int short_k = hq_ozk_short_ok(K);
   CK(hq_ozk_split(w->st, X, xrs, xks, M, K, S, 0, w->ozA, w->ozea));
-  CK(hq_ozk_split(w->st, Y, yrs, yks, N, K, S, 1, w->ozB, w->ozeb));
+  CK(hq_ozk_split(w->st, Y, yrs, yks, N, K, S, short_k ? 2 : 1, w->ozB, w->ozeb));
   prof_mark(w, PH_SPLIT, 0.0);
-  CK(hq_ozk_gemm(w->st, &w->ds->dev, M, N, K, S, w->ozA, w->ozea, w->ozB, w->ozeb, mode, sign, Cm,
-                 crs, ccs, w->ws, w->ws_elems, w->err, spin_limit()));
+  if (short_k)
+    CK(hq_ozk_gemm_short(w->st, &w->ds->dev, M, N, K, S, w->ozA, w->ozea, w->ozB, w->ozeb, mode,
+                         sign, Cm, crs, ccs, w->err, spin_limit()));
+  else
+    CK(hq_ozk_gemm(w->st, &w->ds->dev, M, N, K, S, w->ozA, w->ozea, w->ozB, w->ozeb, mode, sign,
+                   Cm, crs, ccs, w->ws, w->ws_elems, w->err, spin_limit()));
   /* flops charged: the BF16 tensor work, S(S+1)/2 digit products */
   prof_mark(w, PH_TENSOR, (double)S * (S + 1) * M * N * (double)K);
   return HQ_OK;

@@ -49,12 +49,6 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p) {
 // ---------------------------------------------------------------------------
 // Split
 
-// Byte offset of element (row rr, k-in-block kk) inside a 64B-swizzled tile.
-__device__ __forceinline__ int swz64(int rr, int kk) {
-  const int c = kk >> 3;
-  return rr * 64 + ((c ^ ((rr >> 1) & 3)) << 4) + (kk & 7) * 2;
-}
-
 // The fixed-point integer V = round(x * 2^(8S - 1 - e)) of one FP64 entry,
 // computed from its bits (no FP64 arithmetic); |V| <= 2^(8S-1).
 __device__ __forceinline__ long long fixed_point(double x, int shift_base) {
@@ -69,13 +63,26 @@ __device__ __forceinline__ long long fixed_point(double x, int shift_base) {
   return bits < 0 ? -V : V;
 }
 
+// BF16 bit pattern (in the high half of the result) of the digit u - 128 for
+// an integer 0 <= u <= 256: 2^23 + u is exact in FP32, subtracting 2^23 + 128
+// leaves u - 128 exactly, and an integer of at most 8 significant bits has
+// zeros in the low 16 bits of its FP32 pattern.
+__device__ __forceinline__ uint32_t digit_f32(uint32_t u) {
+  return __float_as_uint(__fsub_rn(__uint_as_float(0x4B000000u | u), 8388736.0f));
+}
+
 // Rows r < R of X (element (r, k) at X[r*rs + k*ks], k < K) -> S digit tiles.
 // One warp per row; each lane takes 8-element chunks (one 16-byte group of a
 // tile row), so every digit is written with one 16-byte store.  Rows
-// R..RT*TR-1 and k >= K are written as zeros.
+// R..RT*TR-1 and k >= K are written as zeros.  Balanced base-256 digits come
+// from W = V + 128 * sum_p 256^p: digit p < S-1 is byte p of W minus 128, the
+// top digit W >> 8(S-1) minus 128 (the same digits as peeling them from the
+// bottom); slice s holds digit p = S-1-s, the most significant first.
+template <int S>
 __global__ void ozk_split_kernel(const double* __restrict__ X, long long rs, long long ks, int R,
-                                 int K, int S, int TR, int KB, int rows_total,
+                                 int K, int TR, int KB, int rows_total,
                                  uint8_t* __restrict__ tiles, int* __restrict__ exps) {
+  constexpr unsigned long long BIAS = 0x8080808080808080ULL >> (8 * (8 - S));
   const int lane = threadIdx.x & 31;
   const int warps = blockDim.x >> 5;
   const int nchunk = KB * (TK / 8);
@@ -84,36 +91,51 @@ __global__ void ozk_split_kernel(const double* __restrict__ X, long long rs, lon
        r += gridDim.x * warps) {
     const bool live = r < R;
     const double* xr = X + (live ? (long long)r * rs : 0);
-    double mx = 0.0;
+    // Largest magnitude from the bit patterns (integer compares).
+    long long mb = 0;
     if (live)
-      for (int k = lane; k < K; k += 32) mx = fmax(mx, fabs(xr[(long long)k * ks]));
-    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    int e = 0;
-    if (mx > 0.0) frexp(mx, &e);  // mx < 2^e
+      for (int k = lane; k < K; k += 32) {
+        const long long bb = __double_as_longlong(xr[(long long)k * ks]) & 0x7FFFFFFFFFFFFFFFLL;
+        mb = bb > mb ? bb : mb;
+      }
+    for (int o = 16; o > 0; o >>= 1) {
+      const long long ob = __shfl_xor_sync(0xffffffffu, mb, o);
+      mb = ob > mb ? ob : mb;
+    }
+    // 2^e > max |x| >= 2^(e-1); 0 for zero or subnormal rows.
+    const int bexp = (int)(mb >> 52);
+    const int e = bexp == 0 ? 0 : bexp - 1022;
     if (lane == 0) exps[r] = e;
     const int rt = r / TR, rr = r % TR;
     const int shift_base = 8 * S - 1076 - e;
     for (int ch = lane; ch < nchunk; ch += 32) {
       const int k0 = ch * 8;
-      long long V[8];
+      unsigned long long W[8];
 #pragma unroll
-      for (int j = 0; j < 8; ++j)
-        V[j] = (live && k0 + j < K) ? fixed_point(xr[(long long)(k0 + j) * ks], shift_base) : 0;
+      for (int j = 0; j < 8; ++j) {
+        const long long V =
+            (live && k0 + j < K) ? fixed_point(xr[(long long)(k0 + j) * ks], shift_base) : 0;
+        W[j] = (unsigned long long)V + BIAS;
+      }
       const int kb = k0 / TK, c = (k0 % TK) >> 3;
       uint8_t* base = tiles + ((long long)(rt * KB + kb) * S) * tile_bytes + rr * 64 +
                       ((c ^ ((rr >> 1) & 3)) << 4);
-      // Balanced base-256 digits from the bottom; the top digit takes what is
-      // left, which lies in [-128, 128].
-      for (int s = S - 1; s >= 0; --s) {
+#pragma unroll
+      for (int s = 0; s < S; ++s) {
+        // Slice s holds digit position p = S-1-s (slice 0 the most significant).
+        const int p = S - 1 - s;
         uint32_t w[4];
 #pragma unroll
         for (int j = 0; j < 8; j += 2) {
-          const int d0 = s > 0 ? (int)(((V[j] + 128) & 255) - 128) : (int)V[j];
-          const int d1 = s > 0 ? (int)(((V[j + 1] + 128) & 255) - 128) : (int)V[j + 1];
-          V[j] = (V[j] - d0) >> 8;
-          V[j + 1] = (V[j + 1] - d1) >> 8;
-          const __nv_bfloat162 h = __floats2bfloat162_rn((float)d0, (float)d1);
-          w[j >> 1] = *reinterpret_cast<const uint32_t*>(&h);
+          uint32_t u0, u1;
+          if (p == S - 1) {
+            u0 = (uint32_t)(W[j] >> (8 * p));
+            u1 = (uint32_t)(W[j + 1] >> (8 * p));
+          } else {
+            u0 = (uint32_t)(W[j] >> (8 * p)) & 255u;
+            u1 = (uint32_t)(W[j + 1] >> (8 * p)) & 255u;
+          }
+          w[j >> 1] = __byte_perm(digit_f32(u0), digit_f32(u1), 0x7632);
         }
         *reinterpret_cast<uint4*>(base + (long long)s * tile_bytes) =
             make_uint4(w[0], w[1], w[2], w[3]);
@@ -228,6 +250,21 @@ __device__ __forceinline__ void ff_add(float& hi, float& lo, float x) {
   const float h = __fadd_rn(s, l);
   lo = __fsub_rn(l, __fsub_rn(h, s));
   hi = h;
+}
+
+// An FP32 value times 2^ek (negated when neg) as an FP64, assembled from the
+// bits on the integer pipe -- the FP64 pipe is this GPU's scarce resource and
+// the epilogue of a short-K product would otherwise be bound by it.  Exact for
+// FP32 normals; zero and FP32 subnormals give 0, and so do results below the
+// FP64 normal range (negligible next to the rest of the sum).
+__device__ __forceinline__ double f32_scaled(float f, int ek, unsigned neg) {
+  const unsigned b = __float_as_uint(f);
+  const int ex = (int)((b >> 23) & 0xFF);
+  const int e64 = ex - 127 + 1023 + ek;
+  const unsigned long long bits = ((unsigned long long)((b >> 31) ^ neg) << 63) |
+                                  ((unsigned long long)(e64 & 0x7FF) << 52) |
+                                  ((unsigned long long)(b & 0x7FFFFF) << 29);
+  return (ex == 0 || e64 <= 0) ? 0.0 : __longlong_as_double(bits);
 }
 
 __global__ void __launch_bounds__(NT, 1) ozk_gemm_kernel(OzkArgs a) {
@@ -383,6 +420,7 @@ __global__ void __launch_bounds__(NT, 1) ozk_gemm_kernel(OzkArgs a) {
         const int* __restrict__ ebp = a.eb;
         double* __restrict__ crow = a.C + (long long)r * a.crs + (long long)z * a.zstride;
         const int er = a.ea[r] - 14;
+        const unsigned neg = a.sign < 0.0 ? 1u : 0u;
 #pragma unroll
         for (int c0 = 0; c0 < TN; c0 += 16) {
           int ek[16];
@@ -397,8 +435,9 @@ __global__ void __launch_bounds__(NT, 1) ozk_gemm_kernel(OzkArgs a) {
           for (int j = 0; j < 16; ++j) {
             const int n = nt * TN + c0 + j;
             if (n >= a.N) continue;
-            // hi + lo is exact in FP64; scaling by a power of two is exact.
-            const double v = ldexp(a.sign * ((double)hi[c0 + j] + (double)lo[c0 + j]), ek[j]);
+            // sign * (hi + lo) * 2^ek: the two exact conversions take no FP64
+            // instruction, their sum one (exact: hi + lo fits in FP64).
+            const double v = f32_scaled(hi[c0 + j], ek[j], neg) + f32_scaled(lo[c0 + j], ek[j], neg);
             crow[(long long)n * a.ccs] = a.mode == 0 ? v : cv[j] + v;
           }
         }
@@ -430,6 +469,207 @@ __global__ void __launch_bounds__(NT, 1) ozk_gemm_kernel(OzkArgs a) {
                  : "memory");
 }
 
+// Persistent variant for short products (K <= 256, so no intermediate drain
+// of the exact levels): one CTA per SM walks the output tiles (TM x TNV).  The
+// producer streams operand stages ahead across tile boundaries, and with
+// TNV = 32 the seven level accumulators of a tile (224 TMEM columns) fit
+// twice, so the MMAs of tile i+1 run while the epilogue warps drain tile i.
+// Mode 1 (C += sign * A B^T) or 0 (C = sign * A B^T), no grid.z split.
+template <int TNV>
+__global__ void __launch_bounds__(NT, 1) ozk_gemm_short_kernel(OzkArgs a) {
+  constexpr int B_TILE_V = TNV * TK * 2;
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  __shared__ __align__(8) uint64_t full_bar[MAX_STAGES], empty_bar[MAX_STAGES];
+  __shared__ __align__(8) uint64_t tfull[2], tempty[2], done_bar;
+  __shared__ uint32_t tmem_base;
+  __shared__ volatile int s_abort;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int S = a.S;
+  const int a_stage = S * A_TILE, b_stage = S * B_TILE_V;
+  const uint32_t acc_cols = (uint32_t)(S * TNV);
+  const uint32_t buf_cols = acc_cols <= 32 ? 32u : (acc_cols <= 64 ? 64u : (acc_cols <= 128 ? 128u : 256u));
+  const int nbuf = 2 * buf_cols <= 512 && acc_cols <= 256 ? 2 : 1;
+  const uint32_t tmem_cols = nbuf == 2 ? 2 * buf_cols : 512u;
+  uint8_t* smem = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);
+  const int STAGES = a.stages;
+  uint8_t* sA = smem;
+  uint8_t* sB = smem + STAGES * a_stage;
+  const int MT = (a.M + TM - 1) / TM, NTL = (a.N + TNV - 1) / TNV;
+  const int ntiles = MT * NTL, nkb = a.KB;
+
+  if (tid == 0) {
+    for (int i = 0; i < STAGES; ++i) {
+      mbar_init(&full_bar[i], 1);
+      mbar_init(&empty_bar[i], 1);
+    }
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&tfull[i], 1);
+      mbar_init(&tempty[i], 128);
+    }
+    mbar_init(&done_bar, 1);
+    s_abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_base)),
+                 "r"(tmem_cols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tbase = tmem_base;
+  const unsigned lim = a.spin_limit;
+  int mma_issued = 0;
+  int copies_issued = 0;
+
+  if (warp == 4) {
+    if (lane == 0) {
+      int i = 0;  // stage counter across tiles
+      for (int t = blockIdx.x; t < ntiles && !s_abort; t += gridDim.x) {
+        const int mt = t / NTL, nt = t % NTL;
+        const uint8_t* Ab = a.A + ((long long)mt * a.KB) * a_stage;
+        const uint8_t* Bb = a.B + ((long long)nt * a.KB) * b_stage;
+        for (int kb = 0; kb < nkb; ++kb, ++i) {
+          const int st = i % STAGES;
+          if (!mbar_wait(&empty_bar[st], ((i / STAGES) & 1) ^ 1, lim, &s_abort)) {
+            s_abort = 1;
+            break;
+          }
+          mbar_expect_tx(&full_bar[st], (unsigned)(a_stage + b_stage));
+          bulk_g2s(sA + st * a_stage, Ab + (long long)kb * a_stage, a_stage, &full_bar[st]);
+          bulk_g2s(sB + st * b_stage, Bb + (long long)kb * b_stage, b_stage, &full_bar[st]);
+          ++copies_issued;
+        }
+      }
+    }
+  } else if (warp == 5) {
+    if (lane == 0) {
+      const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TNV >> 3) << 17) |
+                             ((uint32_t)(TM >> 4) << 24);
+      int i = 0, lt = 0;
+      for (int t = blockIdx.x; t < ntiles && !s_abort; t += gridDim.x, ++lt) {
+        const int buf = lt % nbuf;
+        if (!mbar_wait(&tempty[buf], ((lt / nbuf) & 1) ^ 1, lim, &s_abort)) {
+          s_abort = 1;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t tb = tbase + (uint32_t)buf * buf_cols;
+        unsigned fresh = 0xFFu;  // bit L: the next MMA into level L overwrites
+        bool ok = true;
+        for (int kb = 0; kb < nkb; ++kb, ++i) {
+          const int st = i % STAGES;
+          if (!mbar_wait(&full_bar[st], (i / STAGES) & 1, lim, &s_abort)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t abase = smem_u32(sA + st * a_stage), bbase = smem_u32(sB + st * b_stage);
+          for (int s = 0; s < S; ++s) {
+            for (int t2 = 0; s + t2 < S; ++t2) {
+              const int L = s + t2;
+#pragma unroll
+              for (int kk = 0; kk < TK / 16; ++kk) {
+                mma_bf16(tb + (uint32_t)(L * TNV), sw64_desc(abase + s * A_TILE + kk * 32),
+                         sw64_desc(bbase + t2 * B_TILE_V + kk * 32), idesc,
+                         ((fresh >> L) & 1u) ^ 1u);
+                fresh &= ~(1u << L);
+                mma_issued = 1;
+              }
+            }
+          }
+          mma_commit(&empty_bar[st]);
+        }
+        if (!ok) {
+          s_abort = 1;
+          break;
+        }
+        mma_commit(&tfull[buf]);
+      }
+      mma_commit(&done_bar);
+    }
+  } else {
+    // Epilogue warps 0-3: TMEM lanes 32*warp .. 32*warp+31 = tile rows.
+    const uint32_t lane_off = (uint32_t)(warp * 32) << 16;
+    const unsigned neg = a.sign < 0.0 ? 1u : 0u;
+    int lt = 0;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++lt) {
+      const int buf = lt % nbuf;
+      if (!mbar_wait(&tfull[buf], (lt / nbuf) & 1, lim, &s_abort)) {
+        s_abort = 1;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t tb = tbase + (uint32_t)buf * buf_cols + lane_off;
+      const int mt = t / NTL, nt = t % NTL;
+      float hi[TNV], lo[TNV];
+#pragma unroll
+      for (int c = 0; c < TNV; ++c) {
+        hi[c] = 0.f;
+        lo[c] = 0.f;
+      }
+#pragma unroll
+      for (int c0 = 0; c0 < TNV; c0 += 16) {
+        for (int L = 0; L < S; ++L) {
+          float v[16];
+          tmem_ld16(tb + (uint32_t)(L * TNV + c0), v);
+          const float w = __int_as_float((127 - 8 * L) << 23);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) ff_add(hi[c0 + j], lo[c0 + j], __fmul_rn(v[j], w));
+        }
+      }
+      // The accumulators are in registers: hand the TMEM buffer back.
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      mbar_arrive(&tempty[buf]);
+      const int r = mt * TM + warp * 32 + lane;
+      if (r < a.M) {
+        const int* __restrict__ ebp = a.eb;
+        double* __restrict__ crow = a.C + (long long)r * a.crs;
+        const int er = a.ea[r] - 14;
+#pragma unroll
+        for (int c0 = 0; c0 < TNV; c0 += 16) {
+          int ek[16];
+          double cv[16];
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int n = nt * TNV + c0 + j;
+            ek[j] = n < a.N ? er + ebp[n] : 0;
+            cv[j] = (a.mode == 1 && n < a.N) ? crow[(long long)n * a.ccs] : 0.0;
+          }
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int n = nt * TNV + c0 + j;
+            if (n >= a.N) continue;
+            const double v =
+                f32_scaled(hi[c0 + j], ek[j], neg) + f32_scaled(lo[c0 + j], ek[j], neg);
+            crow[(long long)n * a.ccs] = a.mode == 0 ? v : cv[j] + v;
+          }
+        }
+      }
+    }
+  }
+
+  // Teardown: on abort, wait (bounded) for in-flight copies and MMAs first.
+  __syncthreads();
+  if (s_abort) {
+    if (tid == 0) atomicCAS(a.err, 0, HQ_ERR_BARRIER_TIMEOUT);
+    if (warp == 4 && lane == 0) {
+      for (int i = copies_issued > STAGES ? copies_issued - STAGES : 0; i < copies_issued; ++i)
+        mbar_wait(&full_bar[i % STAGES], (i / STAGES) & 1, lim, nullptr);
+    }
+    if (warp == 5 && lane == 0 && mma_issued) mbar_wait(&done_bar, 0, lim, nullptr);
+    __syncthreads();
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase),
+                 "r"(tmem_cols)
+                 : "memory");
+}
+
 __global__ void ozk_sum_slices(int M, int N, int Z, const double* __restrict__ ws,
                                double* __restrict__ C, long long crs, long long ccs, int accumulate) {
   const long long total = (long long)M * N;
@@ -445,8 +685,10 @@ __global__ void ozk_sum_slices(int M, int N, int Z, const double* __restrict__ w
 
 }  // namespace
 
+// side 0: M-side tiles (TM rows); 1: N-side tiles (TN rows) for the general
+// kernel; 2: N-side tiles of 32 rows for the short-K kernel.
 extern "C" size_t hq_ozk_tile_bytes(int rows, int K, int S, int side) {
-  const int TR = side == 0 ? TM : TN;
+  const int TR = side == 0 ? TM : (side == 2 ? 32 : TN);
   const long long RT = (rows + TR - 1) / TR, KB = (K + TK - 1) / TK;
   return (size_t)(RT * KB * S) * (size_t)(TR * TK * 2);
 }
@@ -455,13 +697,22 @@ extern "C" int hq_ozk_split(cudaStream_t stream, const double* X, long long rs, 
                             int R, int K, int S, int side, void* tiles, int* exps) {
   if (R <= 0 || K <= 0) return 0;
   if (S < 1 || S > 7) return (int)cudaErrorInvalidValue;
-  const int TR = side == 0 ? TM : TN;
+  const int TR = side == 0 ? TM : (side == 2 ? 32 : TN);
   const int RT = (R + TR - 1) / TR, KB = (K + TK - 1) / TK;
   const int rows_total = RT * TR;
   int blocks = (rows_total + 7) / 8;
   if (blocks > 4096) blocks = 4096;
-  ozk_split_kernel<<<blocks, 256, 0, stream>>>(X, rs, ks, R, K, S, TR, KB, rows_total,
-                                               static_cast<uint8_t*>(tiles), exps);
+  uint8_t* t = static_cast<uint8_t*>(tiles);
+  switch (S) {
+#define HQ_SPLIT_CASE(SS)                                                                  \
+  case SS:                                                                                 \
+    ozk_split_kernel<SS><<<blocks, 256, 0, stream>>>(X, rs, ks, R, K, TR, KB, rows_total, t, \
+                                                     exps);                                \
+    break;
+    HQ_SPLIT_CASE(1) HQ_SPLIT_CASE(2) HQ_SPLIT_CASE(3) HQ_SPLIT_CASE(4) HQ_SPLIT_CASE(5)
+    HQ_SPLIT_CASE(6) HQ_SPLIT_CASE(7)
+#undef HQ_SPLIT_CASE
+  }
   hq_count_launches(1);
   return (int)cudaGetLastError();
 }
@@ -531,5 +782,51 @@ extern "C" int hq_ozk_gemm(cudaStream_t stream, const hq_device_info* dev, int M
     ozk_sum_slices<<<blocks, 256, 0, stream>>>(M, N, Z, ws, C, crs, ccs, 0);
     hq_count_launches(1);
   }
+  return (int)cudaGetLastError();
+}
+
+// Short products (K <= 256): the persistent double-buffered kernel; B must be
+// split with side 2 (32-row tiles).
+extern "C" int hq_ozk_short_ok(int K) { return K > 0 && K <= KB_PER_DRAIN * TK; }
+
+extern "C" int hq_ozk_gemm_short(cudaStream_t stream, const hq_device_info* dev, int M, int N,
+                                 int K, int S, const void* Atiles, const int* ea,
+                                 const void* Btiles, const int* eb, int mode, double sign,
+                                 double* C, long long crs, long long ccs, int* err,
+                                 unsigned spin_limit) {
+  if (M <= 0 || N <= 0 || K <= 0) return 0;
+  if (S < 1 || S > 7 || !hq_ozk_short_ok(K)) return (int)cudaErrorInvalidValue;
+  constexpr int TNV = 32;
+  OzkArgs a;
+  a.A = static_cast<const uint8_t*>(Atiles);
+  a.B = static_cast<const uint8_t*>(Btiles);
+  a.ea = ea;
+  a.eb = eb;
+  a.M = M;
+  a.N = N;
+  a.S = S;
+  a.KB = (K + TK - 1) / TK;
+  a.kb_per_z = a.KB;
+  a.mode = mode;
+  a.sign = sign;
+  a.err = err;
+  a.spin_limit = spin_limit;
+  a.C = C;
+  a.crs = crs;
+  a.ccs = ccs;
+  a.zstride = 0;
+  const size_t per_stage = (size_t)S * (A_TILE + TNV * TK * 2);
+  int stages = MAX_STAGES;
+  while (stages > 2 && (size_t)stages * per_stage + 1024 > dev->smem_optin) --stages;
+  const size_t smem = (size_t)stages * per_stage + 1024;
+  if (smem > dev->smem_optin) return (int)cudaErrorInvalidValue;
+  a.stages = stages;
+  cudaError_t e = cudaFuncSetAttribute(ozk_gemm_short_kernel<TNV>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return (int)e;
+  const long long tiles = (long long)((M + TM - 1) / TM) * ((N + TNV - 1) / TNV);
+  const int grid = (int)(tiles < dev->num_sms ? tiles : dev->num_sms);
+  ozk_gemm_short_kernel<TNV><<<grid, NT, smem, stream>>>(a);
+  hq_count_launches(1);
   return (int)cudaGetLastError();
 }
