@@ -144,6 +144,85 @@ __global__ void ozk_split_kernel(const double* __restrict__ X, long long rs, lon
   }
 }
 
+// One-pass variant for long rows (4096 <= K <= 16384 with 512 threads): one
+// CTA per row holds the row in registers (CPT chunks of 8 per thread), takes
+// the block maximum and writes the digits, so every entry is read from
+// memory once (the two-pass kernel above re-reads each row, which misses L2
+// when many long rows are in flight).  Same output as the kernel above.
+template <int S, int CPT>
+__global__ void __launch_bounds__(512) ozk_split_row_kernel(
+    const double* __restrict__ X, long long rs, long long ks, int R, int K, int TR, int KB,
+    int rows_total, uint8_t* __restrict__ tiles, int* __restrict__ exps) {
+  constexpr unsigned long long BIAS = 0x8080808080808080ULL >> (8 * (8 - S));
+  constexpr int NTH = 512;
+  __shared__ long long s_max[NTH / 32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nchunk = KB * (TK / 8);
+  const long long tile_bytes = (long long)TR * TK * 2;
+  for (int r = blockIdx.x; r < rows_total; r += gridDim.x) {
+    const bool live = r < R;
+    const double* xr = X + (live ? (long long)r * rs : 0);
+    double v[CPT][8];
+    long long mb = 0;
+#pragma unroll
+    for (int i = 0; i < CPT; ++i) {
+      const int k0 = (tid + i * NTH) * 8;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        v[i][j] = (live && k0 + j < K) ? xr[(long long)(k0 + j) * ks] : 0.0;
+        const long long bb = __double_as_longlong(v[i][j]) & 0x7FFFFFFFFFFFFFFFLL;
+        mb = bb > mb ? bb : mb;
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const long long ob = __shfl_xor_sync(0xffffffffu, mb, o);
+      mb = ob > mb ? ob : mb;
+    }
+    if (lane == 0) s_max[warp] = mb;
+    __syncthreads();
+    mb = s_max[0];
+#pragma unroll
+    for (int w = 1; w < NTH / 32; ++w) mb = s_max[w] > mb ? s_max[w] : mb;
+    __syncthreads();  // s_max is rewritten for the next row
+    const int bexp = (int)(mb >> 52);
+    const int e = bexp == 0 ? 0 : bexp - 1022;
+    if (tid == 0) exps[r] = e;
+    const int rt = r / TR, rr = r % TR;
+    const int shift_base = 8 * S - 1076 - e;
+#pragma unroll
+    for (int i = 0; i < CPT; ++i) {
+      const int ch = tid + i * NTH;
+      if (ch >= nchunk) continue;
+      unsigned long long W[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) W[j] = (unsigned long long)fixed_point(v[i][j], shift_base) + BIAS;
+      const int k0 = ch * 8;
+      const int kb = k0 / TK, c = (k0 % TK) >> 3;
+      uint8_t* base = tiles + ((long long)(rt * KB + kb) * S) * tile_bytes + rr * 64 +
+                      ((c ^ ((rr >> 1) & 3)) << 4);
+#pragma unroll
+      for (int s = 0; s < S; ++s) {
+        const int p = S - 1 - s;
+        uint32_t w[4];
+#pragma unroll
+        for (int j = 0; j < 8; j += 2) {
+          uint32_t u0, u1;
+          if (p == S - 1) {
+            u0 = (uint32_t)(W[j] >> (8 * p));
+            u1 = (uint32_t)(W[j + 1] >> (8 * p));
+          } else {
+            u0 = (uint32_t)(W[j] >> (8 * p)) & 255u;
+            u1 = (uint32_t)(W[j + 1] >> (8 * p)) & 255u;
+          }
+          w[j >> 1] = __byte_perm(digit_f32(u0), digit_f32(u1), 0x7632);
+        }
+        *reinterpret_cast<uint4*>(base + (long long)s * tile_bytes) =
+            make_uint4(w[0], w[1], w[2], w[3]);
+      }
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // GEMM
 
@@ -703,6 +782,14 @@ extern "C" int hq_ozk_split(cudaStream_t stream, const double* X, long long rs, 
   int blocks = (rows_total + 7) / 8;
   if (blocks > 4096) blocks = 4096;
   uint8_t* t = static_cast<uint8_t*>(tiles);
+  constexpr int ROW_CPT = 4;
+  if (K >= 4096 && K <= 512 * 8 * ROW_CPT && S == 7) {
+    int rblocks = rows_total < 16384 ? rows_total : 16384;
+    ozk_split_row_kernel<7, ROW_CPT><<<rblocks, 512, 0, stream>>>(X, rs, ks, R, K, TR, KB,
+                                                                 rows_total, t, exps);
+    hq_count_launches(1);
+    return (int)cudaGetLastError();
+  }
   switch (S) {
 #define HQ_SPLIT_CASE(SS)                                                                  \
   case SS:                                                                                 \
