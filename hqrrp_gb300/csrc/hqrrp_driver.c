@@ -258,6 +258,13 @@ static void ws_release(hq_ws* w) {
 
 /* Workspace for HQRRP on an m x n matrix with block nb + oversampling pp,
  * and for the pivoted / unpivoted panels of dgeqp4 (panel width <= pw). */
+/* N-side digit tiles: the larger of the two tile formats (general and
+ * short-K kernels use different N tiles). */
+static size_t ozk_b_bytes(int rows, int K, int S) {
+  size_t b1 = hq_ozk_tile_bytes(rows, K, S, 1), b2 = hq_ozk_tile_bytes(rows, K, S, 2);
+  return b1 > b2 ? b1 : b2;
+}
+
 static int ws_setup(hq_ws* w, int m, int n, int nb, int pp, int pw) {
   const hq_device_info* dev = &w->ds->dev;
   const int mY = nb + pp;
@@ -300,14 +307,14 @@ static int ws_setup(hq_ws* w, int m, int n, int nb, int pp, int pw) {
   w->bar = ws_alloc(w, sizeof(unsigned) * 2);
   if (w->mixed && mY > 0) {
     const int S = OZK_SLICES, S2 = OZK_SKETCH_SLICES;
-    size_t a = hq_ozk_tile_bytes(n, m, S2, 0), b = hq_ozk_tile_bytes(mY, m, S2, 1), t;
+    size_t a = hq_ozk_tile_bytes(n, m, S2, 0), b = ozk_b_bytes(mY, m, S2), t;
     if ((t = hq_ozk_tile_bytes(kmax, m, S, 0)) > a) a = t;
     if ((t = hq_ozk_tile_bytes(m, kmax, S, 0)) > a) a = t;
     if ((t = hq_ozk_tile_bytes(n, kmax, S, 0)) > a) a = t;
-    if ((t = hq_ozk_tile_bytes(n, m, S, 1)) > b) b = t;
-    if ((t = hq_ozk_tile_bytes(n, kmax, S, 1)) > b) b = t;
-    if ((t = hq_ozk_tile_bytes(mY, m, S, 1)) > b) b = t;
-    if ((t = hq_ozk_tile_bytes(mY, kmax, S, 1)) > b) b = t;
+    if ((t = ozk_b_bytes(n, m, S)) > b) b = t;
+    if ((t = ozk_b_bytes(n, kmax, S)) > b) b = t;
+    if ((t = ozk_b_bytes(mY, m, S)) > b) b = t;
+    if ((t = ozk_b_bytes(mY, kmax, S)) > b) b = t;
     const int rows = imax(imax(m, n), mY) + 128;
     w->ozA = ws_alloc(w, a);
     w->ozB = ws_alloc(w, b);
@@ -866,7 +873,7 @@ HQ_API int hqrrp_gb300_ozaki_dgemm(char transa, char transb, int m, int n, int k
   w.ws_elems = (size_t)8 << 20;
   w.ws = ws_alloc(&w, sizeof(double) * w.ws_elems);
   w.ozA = ws_alloc(&w, hq_ozk_tile_bytes(m, k, slices, 0));
-  w.ozB = ws_alloc(&w, hq_ozk_tile_bytes(n, k, slices, 1));
+  w.ozB = ws_alloc(&w, ozk_b_bytes(n, k, slices));
   w.ozea = ws_alloc(&w, sizeof(int) * (size_t)(m + 128));
   w.ozeb = ws_alloc(&w, sizeof(int) * (size_t)(n + 128));
   w.err = ws_alloc(&w, sizeof(int) * 2);

@@ -8,13 +8,20 @@
 // with integer digits |d_s| <= 128, each exact in BF16.  The product of a
 // digit pair is an integer of at most 2^14 in the pair's unit, so a tensor-
 // core FP32 accumulation of up to 2^24 / (2^14 * pairs) terms is exact.  Pairs
-// are grouped by level L = s + t (same unit 2^(-14-8L)), one TMEM accumulator
-// per level, and only pairs with L <= S-1 are formed (the rest are below the
-// dropped remainder).  Levels 0..3 are exact per 256-deep slice of K and are
-// drained every 256 K into float-float running sums (FP32 pairs, ~48 bits);
-// levels 4 and up are small enough that FP32 rounding there is below the
-// result's precision.  The result is recombined in FP64.  With S = 6 the
-// product is accurate to about 2^-46 relative to |A| |B| row/column-wise.
+// are grouped by level L = s + t (unit 2^(-14-8L)), and only pairs with
+// L <= S-1 are formed (the rest are below the dropped remainder).  Digit s is
+// stored pre-scaled by 2^(-8s) (exact in BF16), so every product already
+// carries its level's weight.  Levels 0..3 each get a TMEM accumulator, exact
+// per 256-deep slice of K (integers below 2^24 in their unit); level 4 gets its
+// own; levels 5 and 6 need at most 2^-12 relative precision and share one.
+// All are drained every 256 K into float-float running sums (FP32 pairs, ~48
+// bits).  (Folding level 4 in as well measured 2^-47.5 instead of 2^-52: the
+// tensor core's FP32 accumulation loses more than IEEE rounding when products
+// of very different magnitude meet in one accumulator.)  Six accumulators
+// instead of seven leave TMEM room for 80-column tiles in the short-K kernel --
+// a tcgen05 BF16 MMA takes the same time for N = 64 as for N = 128.  The
+// result is recombined in FP64.  With S = 7 the product is accurate to about
+// 2^-52 relative to |A| |B| row/column-wise.
 //
 // Layout: operands are pre-split by ozk_split_kernel into K-major BF16 tiles
 // already in the 64-byte-swizzled shared-memory order the MMA reads (rows of
@@ -34,13 +41,25 @@
 
 namespace {
 
-constexpr int TM = 128, TN = 64, TK = 32;
+constexpr int TM = 128, TN = 80, TK = 32;  // six accumulators x 80 = 480 TMEM columns
+constexpr int TN_SHORT = TN;  // the short-K kernel uses the same N tiles
 constexpr int MAX_STAGES = 3;
 constexpr int KB_PER_DRAIN = 8;  // 256 K elements
-constexpr int EXACT_LEVELS = 4;
-constexpr int NT = 192;  // warps 0-3 epilogue, 4 producer, 5 MMA
+constexpr int MAX_ACC = 6;  // levels 0..4 alone (0..3 exact), 5 and 6 shared
+
+__host__ __device__ constexpr int n_acc(int S) { return S < MAX_ACC ? S : MAX_ACC; }
+__device__ __forceinline__ int acc_of_level(int L) { return L < MAX_ACC - 1 ? L : MAX_ACC - 1; }
+__host__ __device__ inline uint32_t tmem_pow2(uint32_t c) {
+  return c <= 32 ? 32u : (c <= 64 ? 64u : (c <= 128 ? 128u : (c <= 256 ? 256u : 512u)));
+}
+// Warps 0-7 epilogue (two per TMEM lane quadrant, each half of the tile's
+// columns), warp 8 producer, warp 9 MMA.
+constexpr int NT = 320;
+constexpr int NEPI = 256;
+constexpr int PRODUCER_WARP = 8, MMA_WARP = 9;
+constexpr int EPI_COLS = TN / 2;  // columns per epilogue thread
 constexpr int A_TILE = TM * TK * 2;  // 8 KB per digit tile
-constexpr int B_TILE = TN * TK * 2;  // 4 KB per digit tile
+constexpr int B_TILE = TN * TK * 2;  // 5 KB per digit tile
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -69,6 +88,12 @@ __device__ __forceinline__ long long fixed_point(double x, int shift_base) {
 // zeros in the low 16 bits of its FP32 pattern.
 __device__ __forceinline__ uint32_t digit_f32(uint32_t u) {
   return __float_as_uint(__fsub_rn(__uint_as_float(0x4B000000u | u), 8388736.0f));
+}
+
+// The same digit times 2^(-8s) for slice s (exact: a power-of-two scale of a
+// small integer), so that products carry their level's weight.
+__device__ __forceinline__ uint32_t digit_scaled(uint32_t u, int s) {
+  return __float_as_uint(__fmul_rn(__uint_as_float(digit_f32(u)), __int_as_float((127 - 8 * s) << 23)));
 }
 
 // Rows r < R of X (element (r, k) at X[r*rs + k*ks], k < K) -> S digit tiles.
@@ -135,7 +160,7 @@ __global__ void ozk_split_kernel(const double* __restrict__ X, long long rs, lon
             u0 = (uint32_t)(W[j] >> (8 * p)) & 255u;
             u1 = (uint32_t)(W[j + 1] >> (8 * p)) & 255u;
           }
-          w[j >> 1] = __byte_perm(digit_f32(u0), digit_f32(u1), 0x7632);
+          w[j >> 1] = __byte_perm(digit_scaled(u0, s), digit_scaled(u1, s), 0x7632);
         }
         *reinterpret_cast<uint4*>(base + (long long)s * tile_bytes) =
             make_uint4(w[0], w[1], w[2], w[3]);
@@ -214,7 +239,7 @@ __global__ void __launch_bounds__(512) ozk_split_row_kernel(
             u0 = (uint32_t)(W[j] >> (8 * p)) & 255u;
             u1 = (uint32_t)(W[j + 1] >> (8 * p)) & 255u;
           }
-          w[j >> 1] = __byte_perm(digit_f32(u0), digit_f32(u1), 0x7632);
+          w[j >> 1] = __byte_perm(digit_scaled(u0, s), digit_scaled(u1, s), 0x7632);
         }
         *reinterpret_cast<uint4*>(base + (long long)s * tile_bytes) =
             make_uint4(w[0], w[1], w[2], w[3]);
@@ -307,17 +332,18 @@ __device__ __forceinline__ void mma_commit(uint64_t* b) {
                : "memory");
 }
 
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
-  uint32_t r[16];
+// 8 consecutive TMEM columns of this warp's 32 lanes.
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
+  uint32_t r[8];
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+      "tcgen05.wait::ld.sync.aligned;"
       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-        "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        "=r"(r[7])
+      : "r"(taddr)
+      : "memory");
 #pragma unroll
-  for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+  for (int j = 0; j < 8; ++j) v[j] = __uint_as_float(r[j]);
 }
 
 // (hi, lo) += x in FP32 pairs (TwoSum, then renormalise).
@@ -346,6 +372,76 @@ __device__ __forceinline__ double f32_scaled(float f, int ek, unsigned neg) {
   return (ex == 0 || e64 <= 0) ? 0.0 : __longlong_as_double(bits);
 }
 
+// Epilogue thread's share of a tile: TMEM lanes of its quadrant (one output
+// row each), EPI_COLS columns starting at col0.  Adds the nacc accumulators
+// of those columns into the float-float running sums.
+__device__ __forceinline__ void drain_tmem(uint32_t tacc, int nacc, float* hi, float* lo) {
+#pragma unroll
+  for (int c8 = 0; c8 < EPI_COLS; c8 += 8) {
+    for (int q = 0; q < nacc; ++q) {
+      float v[8];
+      tmem_ld8(tacc + (uint32_t)(q * TN + c8), v);
+#pragma unroll
+      for (int j = 0; j < 8; ++j) ff_add(hi[c8 + j], lo[c8 + j], v[j]);
+    }
+  }
+}
+
+// Output of one row's EPI_COLS columns: out = sign * (hi + lo) * 2^(ea + eb - 14)
+// (mode 0) or C += that (mode 1).  In update mode the row's C entries are
+// first prefetched into L2 (no registers held), then read in batches of 8
+// with every load of a batch issued before its stores.
+__device__ __forceinline__ void write_row(const OzkArgs& a, int r, int n0, double* crow,
+                                          const float* hi, const float* lo) {
+  const unsigned neg = a.sign < 0.0 ? 1u : 0u;
+  const int er = a.ea[r] - 14;
+  if (a.mode == 1) {
+#pragma unroll
+    for (int j = 0; j < EPI_COLS; ++j)
+      if (n0 + j < a.N)
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(crow + (long long)(n0 + j) * a.ccs));
+  }
+#pragma unroll
+  for (int c8 = 0; c8 < EPI_COLS; c8 += 8) {
+    double cv[8];
+    int ek[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int n = n0 + c8 + j;
+      ek[j] = n < a.N ? er + a.eb[n] : 0;
+      cv[j] = (a.mode == 1 && n < a.N) ? crow[(long long)n * a.ccs] : 0.0;
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int n = n0 + c8 + j;
+      if (n < a.N) {
+        // sign * (hi + lo) * 2^ek: the two exact conversions take no FP64
+        // instruction, their sum one (exact: hi + lo fits in FP64).
+        const double v = f32_scaled(hi[c8 + j], ek[j], neg) + f32_scaled(lo[c8 + j], ek[j], neg);
+        crow[(long long)n * a.ccs] = a.mode == 0 ? v : cv[j] + v;
+      }
+    }
+  }
+}
+
+// Digit-pair MMAs of one K block into the accumulators at tb: pair (s, t) into
+// acc_of_level(s + t).  fresh: bit q set = the next MMA into q overwrites.
+__device__ __forceinline__ void issue_block(uint32_t tb, uint64_t da0, uint64_t db0, int S,
+                                            uint32_t idesc, unsigned& fresh) {
+  for (int s = 0; s < S; ++s) {
+    const uint64_t da = da0 + (uint64_t)((s * A_TILE) >> 4);  // start address advances by bytes >> 4
+    for (int t = 0; s + t < S; ++t) {
+      const int q = acc_of_level(s + t);
+      const uint64_t db = db0 + (uint64_t)((t * B_TILE) >> 4);
+#pragma unroll
+      for (int kk = 0; kk < TK / 16; ++kk) {
+        mma_bf16(tb + (uint32_t)(q * TN), da + 2 * kk, db + 2 * kk, idesc, ((fresh >> q) & 1u) ^ 1u);
+        fresh &= ~(1u << q);
+      }
+    }
+  }
+}
+
 __global__ void __launch_bounds__(NT, 1) ozk_gemm_kernel(OzkArgs a) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   __shared__ __align__(8) uint64_t full_bar[MAX_STAGES], empty_bar[MAX_STAGES];
@@ -355,8 +451,8 @@ __global__ void __launch_bounds__(NT, 1) ozk_gemm_kernel(OzkArgs a) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int S = a.S;
   const int a_stage = S * A_TILE, b_stage = S * B_TILE;
-  // One TN-column accumulator per level, rounded up to a power of two.
-  const uint32_t tmem_cols = S * TN <= 64 ? 64u : (S * TN <= 128 ? 128u : (S * TN <= 256 ? 256u : 512u));
+  const int nacc = n_acc(S);
+  const uint32_t tmem_cols = tmem_pow2((uint32_t)(nacc * TN));
   uint8_t* smem = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);
   uint8_t* sA = smem;
   const int STAGES = a.stages;
@@ -372,7 +468,7 @@ __global__ void __launch_bounds__(NT, 1) ozk_gemm_kernel(OzkArgs a) {
       mbar_init(&empty_bar[i], 1);
     }
     mbar_init(&drain_full, 1);
-    mbar_init(&drain_empty, 128);
+    mbar_init(&drain_empty, NEPI);
     mbar_init(&done_bar, 1);
     s_abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -391,7 +487,7 @@ __global__ void __launch_bounds__(NT, 1) ozk_gemm_kernel(OzkArgs a) {
   int mma_issued = 0;  // MMA thread: any tcgen05.mma issued
   int copies_issued = 0;
 
-  if (warp == 4) {
+  if (warp == PRODUCER_WARP) {
     // Producer: one elected lane streams the digit tiles through the ring.
     if (lane == 0) {
       const uint8_t* Ab = a.A + ((long long)mt * a.KB) * a_stage;
@@ -408,11 +504,11 @@ __global__ void __launch_bounds__(NT, 1) ozk_gemm_kernel(OzkArgs a) {
         ++copies_issued;
       }
     }
-  } else if (warp == 5) {
+  } else if (warp == MMA_WARP) {
     if (lane == 0) {
       const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TN >> 3) << 17) |
                              ((uint32_t)(TM >> 4) << 24);
-      unsigned fresh = 0xFFu;  // bit L: the next MMA into level L overwrites
+      unsigned fresh = 0xFFu;
       int d = 0;
       for (int i = 0; i < nkb; ++i) {
         const int st = i % STAGES;
@@ -421,20 +517,9 @@ __global__ void __launch_bounds__(NT, 1) ozk_gemm_kernel(OzkArgs a) {
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t abase = smem_u32(sA + st * a_stage), bbase = smem_u32(sB + st * b_stage);
-        for (int s = 0; s < S; ++s) {
-          for (int t = 0; s + t < S; ++t) {
-            const int L = s + t;
-            const uint32_t dt = tbase + (uint32_t)(L * TN);
-#pragma unroll
-            for (int kk = 0; kk < TK / 16; ++kk) {
-              mma_bf16(dt, sw64_desc(abase + s * A_TILE + kk * 32),
-                       sw64_desc(bbase + t * B_TILE + kk * 32), idesc, ((fresh >> L) & 1u) ^ 1u);
-              fresh &= ~(1u << L);
-              mma_issued = 1;
-            }
-          }
-        }
+        issue_block(tbase, sw64_desc(smem_u32(sA + st * a_stage)),
+                    sw64_desc(smem_u32(sB + st * b_stage)), S, idesc, fresh);
+        mma_issued = 1;
         mma_commit(&empty_bar[st]);
         if ((i + 1) % KB_PER_DRAIN == 0 && i + 1 < nkb) {
           mma_commit(&drain_full);
@@ -443,36 +528,28 @@ __global__ void __launch_bounds__(NT, 1) ozk_gemm_kernel(OzkArgs a) {
             break;
           }
           ++d;
-          fresh |= (1u << EXACT_LEVELS) - 1u;
+          fresh = 0xFFu;  // every accumulator restarts after a drain
         }
       }
       mma_commit(&done_bar);
     }
   } else {
-    // Epilogue warps 0-3: TMEM lanes 32*warp .. 32*warp+31 = tile rows.
-    float hi[TN], lo[TN];
+    // Epilogue warps 0-7: TMEM lanes 32*(warp&3).. = tile rows, columns
+    // (warp>>2)*EPI_COLS.. of the tile.
+    float hi[EPI_COLS], lo[EPI_COLS];
 #pragma unroll
-    for (int c = 0; c < TN; ++c) {
+    for (int c = 0; c < EPI_COLS; ++c) {
       hi[c] = 0.f;
       lo[c] = 0.f;
     }
-    const uint32_t lane_off = (uint32_t)(warp * 32) << 16;
+    const int col0 = (warp >> 2) * EPI_COLS;
+    const uint32_t tacc = tbase + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)col0;
     bool ok = true;
     for (int d = 0; d < ndrain && ok; ++d) {
       ok = mbar_wait(&drain_full, d & 1, lim, &s_abort);
       if (!ok) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const int nl = min(S, EXACT_LEVELS);
-#pragma unroll
-      for (int c0 = 0; c0 < TN; c0 += 16) {
-        for (int L = 0; L < nl; ++L) {
-          float v[16];
-          tmem_ld16(tbase + lane_off + (uint32_t)(L * TN + c0), v);
-          const float w = __int_as_float((127 - 8 * L) << 23);  // 2^(-8L)
-#pragma unroll
-          for (int j = 0; j < 16; ++j) ff_add(hi[c0 + j], lo[c0 + j], __fmul_rn(v[j], w));
-        }
-      }
+      drain_tmem(tacc, nacc, hi, lo);
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       mbar_arrive(&drain_empty);
     }
@@ -481,46 +558,11 @@ __global__ void __launch_bounds__(NT, 1) ozk_gemm_kernel(OzkArgs a) {
       s_abort = 1;
     } else {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-#pragma unroll
-      for (int c0 = 0; c0 < TN; c0 += 16) {
-        for (int L = 0; L < S; ++L) {
-          float v[16];
-          tmem_ld16(tbase + lane_off + (uint32_t)(L * TN + c0), v);
-          const float w = __int_as_float((127 - 8 * L) << 23);
-#pragma unroll
-          for (int j = 0; j < 16; ++j) ff_add(hi[c0 + j], lo[c0 + j], __fmul_rn(v[j], w));
-        }
-      }
-      const int r = mt * TM + warp * 32 + lane;
-      if (r < a.M) {
-        // Output in chunks of 16 columns: every load (column scales, and C in
-        // update mode) of a chunk is issued before any store, so the loads of
-        // a chunk overlap instead of each waiting behind the previous store.
-        const int* __restrict__ ebp = a.eb;
-        double* __restrict__ crow = a.C + (long long)r * a.crs + (long long)z * a.zstride;
-        const int er = a.ea[r] - 14;
-        const unsigned neg = a.sign < 0.0 ? 1u : 0u;
-#pragma unroll
-        for (int c0 = 0; c0 < TN; c0 += 16) {
-          int ek[16];
-          double cv[16];
-#pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const int n = nt * TN + c0 + j;
-            ek[j] = n < a.N ? er + ebp[n] : 0;
-            cv[j] = (a.mode == 1 && n < a.N) ? crow[(long long)n * a.ccs] : 0.0;
-          }
-#pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const int n = nt * TN + c0 + j;
-            if (n >= a.N) continue;
-            // sign * (hi + lo) * 2^ek: the two exact conversions take no FP64
-            // instruction, their sum one (exact: hi + lo fits in FP64).
-            const double v = f32_scaled(hi[c0 + j], ek[j], neg) + f32_scaled(lo[c0 + j], ek[j], neg);
-            crow[(long long)n * a.ccs] = a.mode == 0 ? v : cv[j] + v;
-          }
-        }
-      }
+      drain_tmem(tacc, nacc, hi, lo);
+      const int r = mt * TM + (warp & 3) * 32 + lane;
+      if (r < a.M)
+        write_row(a, r, nt * TN + col0, a.C + (long long)r * a.crs + (long long)z * a.zstride, hi,
+                  lo);
     }
   }
 
@@ -528,13 +570,13 @@ __global__ void __launch_bounds__(NT, 1) ozk_gemm_kernel(OzkArgs a) {
   __syncthreads();
   if (s_abort) {
     if (tid == 0) atomicCAS(a.err, 0, HQ_ERR_BARRIER_TIMEOUT);
-    if (warp == 4 && lane == 0) {
+    if (warp == PRODUCER_WARP && lane == 0) {
       // The last copy issued into each stage is the only one that can still
       // be in flight.
       for (int i = copies_issued > STAGES ? copies_issued - STAGES : 0; i < copies_issued; ++i)
         mbar_wait(&full_bar[i % STAGES], (i / STAGES) & 1, lim, nullptr);
     }
-    if (warp == 5 && lane == 0 && mma_issued) {
+    if (warp == MMA_WARP && lane == 0 && mma_issued) {
       // done_bar was committed after the loop; its completion covers all MMAs.
       mbar_wait(&done_bar, 0, lim, nullptr);
     }
@@ -549,31 +591,28 @@ __global__ void __launch_bounds__(NT, 1) ozk_gemm_kernel(OzkArgs a) {
 }
 
 // Persistent variant for short products (K <= 256, so no intermediate drain
-// of the exact levels): one CTA per SM walks the output tiles (TM x TNV).  The
-// producer streams operand stages ahead across tile boundaries, and with
-// TNV = 32 the seven level accumulators of a tile (224 TMEM columns) fit
-// twice, so the MMAs of tile i+1 run while the epilogue warps drain tile i.
-// Mode 1 (C += sign * A B^T) or 0 (C = sign * A B^T), no grid.z split.
-template <int TNV>
+// of the exact levels): one CTA per SM walks the output tiles (TM x TN), and
+// the producer streams operand stages ahead across tile boundaries.  The
+// epilogue warps first drain a tile's accumulators into registers and hand
+// the TMEM back, then do the FP64 output (the part bound by the FP64 pipe and
+// by C's memory traffic) while the MMAs of the next tile run.  Mode 1
+// (C += sign * A B^T) or 0 (C = sign * A B^T), no grid.z split.
 __global__ void __launch_bounds__(NT, 1) ozk_gemm_short_kernel(OzkArgs a) {
-  constexpr int B_TILE_V = TNV * TK * 2;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   __shared__ __align__(8) uint64_t full_bar[MAX_STAGES], empty_bar[MAX_STAGES];
-  __shared__ __align__(8) uint64_t tfull[2], tempty[2], done_bar;
+  __shared__ __align__(8) uint64_t tfull, tempty, done_bar;
   __shared__ uint32_t tmem_base;
   __shared__ volatile int s_abort;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int S = a.S;
-  const int a_stage = S * A_TILE, b_stage = S * B_TILE_V;
-  const uint32_t acc_cols = (uint32_t)(S * TNV);
-  const uint32_t buf_cols = acc_cols <= 32 ? 32u : (acc_cols <= 64 ? 64u : (acc_cols <= 128 ? 128u : 256u));
-  const int nbuf = 2 * buf_cols <= 512 && acc_cols <= 256 ? 2 : 1;
-  const uint32_t tmem_cols = nbuf == 2 ? 2 * buf_cols : 512u;
+  const int a_stage = S * A_TILE, b_stage = S * B_TILE;
+  const int nacc = n_acc(S);
+  const uint32_t tmem_cols = tmem_pow2((uint32_t)(nacc * TN));
   uint8_t* smem = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);
   const int STAGES = a.stages;
   uint8_t* sA = smem;
   uint8_t* sB = smem + STAGES * a_stage;
-  const int MT = (a.M + TM - 1) / TM, NTL = (a.N + TNV - 1) / TNV;
+  const int MT = (a.M + TM - 1) / TM, NTL = (a.N + TN - 1) / TN;
   const int ntiles = MT * NTL, nkb = a.KB;
 
   if (tid == 0) {
@@ -581,10 +620,8 @@ __global__ void __launch_bounds__(NT, 1) ozk_gemm_short_kernel(OzkArgs a) {
       mbar_init(&full_bar[i], 1);
       mbar_init(&empty_bar[i], 1);
     }
-    for (int i = 0; i < 2; ++i) {
-      mbar_init(&tfull[i], 1);
-      mbar_init(&tempty[i], 128);
-    }
+    mbar_init(&tfull, 1);
+    mbar_init(&tempty, NEPI);
     mbar_init(&done_bar, 1);
     s_abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -603,7 +640,7 @@ __global__ void __launch_bounds__(NT, 1) ozk_gemm_short_kernel(OzkArgs a) {
   int mma_issued = 0;
   int copies_issued = 0;
 
-  if (warp == 4) {
+  if (warp == PRODUCER_WARP) {
     if (lane == 0) {
       int i = 0;  // stage counter across tiles
       for (int t = blockIdx.x; t < ntiles && !s_abort; t += gridDim.x) {
@@ -623,20 +660,18 @@ __global__ void __launch_bounds__(NT, 1) ozk_gemm_short_kernel(OzkArgs a) {
         }
       }
     }
-  } else if (warp == 5) {
+  } else if (warp == MMA_WARP) {
     if (lane == 0) {
-      const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TNV >> 3) << 17) |
+      const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TN >> 3) << 17) |
                              ((uint32_t)(TM >> 4) << 24);
       int i = 0, lt = 0;
       for (int t = blockIdx.x; t < ntiles && !s_abort; t += gridDim.x, ++lt) {
-        const int buf = lt % nbuf;
-        if (!mbar_wait(&tempty[buf], ((lt / nbuf) & 1) ^ 1, lim, &s_abort)) {
+        if (!mbar_wait(&tempty, (lt & 1) ^ 1, lim, &s_abort)) {
           s_abort = 1;
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t tb = tbase + (uint32_t)buf * buf_cols;
-        unsigned fresh = 0xFFu;  // bit L: the next MMA into level L overwrites
+        unsigned fresh = 0xFFu;
         bool ok = true;
         for (int kb = 0; kb < nkb; ++kb, ++i) {
           const int st = i % STAGES;
@@ -645,88 +680,42 @@ __global__ void __launch_bounds__(NT, 1) ozk_gemm_short_kernel(OzkArgs a) {
             break;
           }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-          const uint32_t abase = smem_u32(sA + st * a_stage), bbase = smem_u32(sB + st * b_stage);
-          for (int s = 0; s < S; ++s) {
-            for (int t2 = 0; s + t2 < S; ++t2) {
-              const int L = s + t2;
-#pragma unroll
-              for (int kk = 0; kk < TK / 16; ++kk) {
-                mma_bf16(tb + (uint32_t)(L * TNV), sw64_desc(abase + s * A_TILE + kk * 32),
-                         sw64_desc(bbase + t2 * B_TILE_V + kk * 32), idesc,
-                         ((fresh >> L) & 1u) ^ 1u);
-                fresh &= ~(1u << L);
-                mma_issued = 1;
-              }
-            }
-          }
+          issue_block(tbase, sw64_desc(smem_u32(sA + st * a_stage)),
+                      sw64_desc(smem_u32(sB + st * b_stage)), S, idesc, fresh);
+          mma_issued = 1;
           mma_commit(&empty_bar[st]);
         }
         if (!ok) {
           s_abort = 1;
           break;
         }
-        mma_commit(&tfull[buf]);
+        mma_commit(&tfull);
       }
       mma_commit(&done_bar);
     }
   } else {
-    // Epilogue warps 0-3: TMEM lanes 32*warp .. 32*warp+31 = tile rows.
-    const uint32_t lane_off = (uint32_t)(warp * 32) << 16;
-    const unsigned neg = a.sign < 0.0 ? 1u : 0u;
+    const int col0 = (warp >> 2) * EPI_COLS;
+    const uint32_t tacc = tbase + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)col0;
     int lt = 0;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++lt) {
-      const int buf = lt % nbuf;
-      if (!mbar_wait(&tfull[buf], (lt / nbuf) & 1, lim, &s_abort)) {
+      if (!mbar_wait(&tfull, lt & 1, lim, &s_abort)) {
         s_abort = 1;
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t tb = tbase + (uint32_t)buf * buf_cols + lane_off;
-      const int mt = t / NTL, nt = t % NTL;
-      float hi[TNV], lo[TNV];
+      float hi[EPI_COLS], lo[EPI_COLS];
 #pragma unroll
-      for (int c = 0; c < TNV; ++c) {
+      for (int c = 0; c < EPI_COLS; ++c) {
         hi[c] = 0.f;
         lo[c] = 0.f;
       }
-#pragma unroll
-      for (int c0 = 0; c0 < TNV; c0 += 16) {
-        for (int L = 0; L < S; ++L) {
-          float v[16];
-          tmem_ld16(tb + (uint32_t)(L * TNV + c0), v);
-          const float w = __int_as_float((127 - 8 * L) << 23);
-#pragma unroll
-          for (int j = 0; j < 16; ++j) ff_add(hi[c0 + j], lo[c0 + j], __fmul_rn(v[j], w));
-        }
-      }
-      // The accumulators are in registers: hand the TMEM buffer back.
+      drain_tmem(tacc, nacc, hi, lo);
+      // The sums are in registers: hand the TMEM back for the next tile.
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      mbar_arrive(&tempty[buf]);
-      const int r = mt * TM + warp * 32 + lane;
-      if (r < a.M) {
-        const int* __restrict__ ebp = a.eb;
-        double* __restrict__ crow = a.C + (long long)r * a.crs;
-        const int er = a.ea[r] - 14;
-#pragma unroll
-        for (int c0 = 0; c0 < TNV; c0 += 16) {
-          int ek[16];
-          double cv[16];
-#pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const int n = nt * TNV + c0 + j;
-            ek[j] = n < a.N ? er + ebp[n] : 0;
-            cv[j] = (a.mode == 1 && n < a.N) ? crow[(long long)n * a.ccs] : 0.0;
-          }
-#pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const int n = nt * TNV + c0 + j;
-            if (n >= a.N) continue;
-            const double v =
-                f32_scaled(hi[c0 + j], ek[j], neg) + f32_scaled(lo[c0 + j], ek[j], neg);
-            crow[(long long)n * a.ccs] = a.mode == 0 ? v : cv[j] + v;
-          }
-        }
-      }
+      mbar_arrive(&tempty);
+      const int mt = t / NTL, nt = t % NTL;
+      const int r = mt * TM + (warp & 3) * 32 + lane;
+      if (r < a.M) write_row(a, r, nt * TN + col0, a.C + (long long)r * a.crs, hi, lo);
     }
   }
 
@@ -734,11 +723,11 @@ __global__ void __launch_bounds__(NT, 1) ozk_gemm_short_kernel(OzkArgs a) {
   __syncthreads();
   if (s_abort) {
     if (tid == 0) atomicCAS(a.err, 0, HQ_ERR_BARRIER_TIMEOUT);
-    if (warp == 4 && lane == 0) {
+    if (warp == PRODUCER_WARP && lane == 0) {
       for (int i = copies_issued > STAGES ? copies_issued - STAGES : 0; i < copies_issued; ++i)
         mbar_wait(&full_bar[i % STAGES], (i / STAGES) & 1, lim, nullptr);
     }
-    if (warp == 5 && lane == 0 && mma_issued) mbar_wait(&done_bar, 0, lim, nullptr);
+    if (warp == MMA_WARP && lane == 0 && mma_issued) mbar_wait(&done_bar, 0, lim, nullptr);
     __syncthreads();
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -765,9 +754,9 @@ __global__ void ozk_sum_slices(int M, int N, int Z, const double* __restrict__ w
 }  // namespace
 
 // side 0: M-side tiles (TM rows); 1: N-side tiles (TN rows) for the general
-// kernel; 2: N-side tiles of 32 rows for the short-K kernel.
+// kernel; 2: N-side tiles of TN_SHORT rows for the short-K kernel.
 extern "C" size_t hq_ozk_tile_bytes(int rows, int K, int S, int side) {
-  const int TR = side == 0 ? TM : (side == 2 ? 32 : TN);
+  const int TR = side == 0 ? TM : (side == 2 ? TN_SHORT : TN);
   const long long RT = (rows + TR - 1) / TR, KB = (K + TK - 1) / TK;
   return (size_t)(RT * KB * S) * (size_t)(TR * TK * 2);
 }
@@ -776,7 +765,7 @@ extern "C" int hq_ozk_split(cudaStream_t stream, const double* X, long long rs, 
                             int R, int K, int S, int side, void* tiles, int* exps) {
   if (R <= 0 || K <= 0) return 0;
   if (S < 1 || S > 7) return (int)cudaErrorInvalidValue;
-  const int TR = side == 0 ? TM : (side == 2 ? 32 : TN);
+  const int TR = side == 0 ? TM : (side == 2 ? TN_SHORT : TN);
   const int RT = (R + TR - 1) / TR, KB = (K + TK - 1) / TK;
   const int rows_total = RT * TR;
   int blocks = (rows_total + 7) / 8;
@@ -872,8 +861,8 @@ extern "C" int hq_ozk_gemm(cudaStream_t stream, const hq_device_info* dev, int M
   return (int)cudaGetLastError();
 }
 
-// Short products (K <= 256): the persistent double-buffered kernel; B must be
-// split with side 2 (32-row tiles).
+// Short products (K <= 256): the persistent kernel; B must be split with side
+// 2 (TN_SHORT-row tiles).
 extern "C" int hq_ozk_short_ok(int K) { return K > 0 && K <= KB_PER_DRAIN * TK; }
 
 extern "C" int hq_ozk_gemm_short(cudaStream_t stream, const hq_device_info* dev, int M, int N,
@@ -883,7 +872,7 @@ extern "C" int hq_ozk_gemm_short(cudaStream_t stream, const hq_device_info* dev,
                                  unsigned spin_limit) {
   if (M <= 0 || N <= 0 || K <= 0) return 0;
   if (S < 1 || S > 7 || !hq_ozk_short_ok(K)) return (int)cudaErrorInvalidValue;
-  constexpr int TNV = 32;
+  constexpr int TNV = TN_SHORT;
   OzkArgs a;
   a.A = static_cast<const uint8_t*>(Atiles);
   a.B = static_cast<const uint8_t*>(Btiles);
@@ -902,18 +891,18 @@ extern "C" int hq_ozk_gemm_short(cudaStream_t stream, const hq_device_info* dev,
   a.crs = crs;
   a.ccs = ccs;
   a.zstride = 0;
-  const size_t per_stage = (size_t)S * (A_TILE + TNV * TK * 2);
+  const size_t per_stage = (size_t)S * (A_TILE + B_TILE);
   int stages = MAX_STAGES;
   while (stages > 2 && (size_t)stages * per_stage + 1024 > dev->smem_optin) --stages;
   const size_t smem = (size_t)stages * per_stage + 1024;
   if (smem > dev->smem_optin) return (int)cudaErrorInvalidValue;
   a.stages = stages;
-  cudaError_t e = cudaFuncSetAttribute(ozk_gemm_short_kernel<TNV>,
+  cudaError_t e = cudaFuncSetAttribute(ozk_gemm_short_kernel,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return (int)e;
   const long long tiles = (long long)((M + TM - 1) / TM) * ((N + TNV - 1) / TNV);
   const int grid = (int)(tiles < dev->num_sms ? tiles : dev->num_sms);
-  ozk_gemm_short_kernel<TNV><<<grid, NT, smem, stream>>>(a);
+  ozk_gemm_short_kernel<<<grid, NT, smem, stream>>>(a);
   hq_count_launches(1);
   return (int)cudaGetLastError();
 }
