@@ -49,7 +49,7 @@ int hq_sketch_philox(cudaStream_t stream, int rows, int cols, double* G, int ldg
 int hq_skinny_qrp(cudaStream_t stream, const hq_device_info* dev, int mY, int N, int b,
                   const double* Y, int ldy, double* V, int ldv, int* pairs, int* npairs,
                   double* part, size_t part_elems, unsigned* bar, int* err,
-                  unsigned spin_limit);
+                  unsigned spin_limit, int fp32);
 size_t hq_skinny_part_elems(const hq_device_info* dev, int mY);
 
 /* ---- Panel: pivoted (or plain) QR of the mp x nc block P (ldp) ---------

@@ -315,6 +315,8 @@ static int ws_setup(hq_ws* w, int m, int n, int nb, int pp, int pw) {
     if ((t = ozk_b_bytes(n, kmax, S)) > b) b = t;
     if ((t = ozk_b_bytes(mY, m, S)) > b) b = t;
     if ((t = ozk_b_bytes(mY, kmax, S)) > b) b = t;
+    if ((t = hq_ozk_tile_bytes(mY, kmax, S, 0)) > a) a = t; /* B2 = Bm T */
+    if ((t = ozk_b_bytes(kmax, kmax, S)) > b) b = t;
     const int rows = imax(imax(m, n), mY) + 128;
     w->ozA = ws_alloc(w, a);
     w->ozB = ws_alloc(w, b);
@@ -372,16 +374,21 @@ static int ozk_product(hq_ws* w, int S, int M, int N, int K, const double* X, lo
 static int block_reflector(hq_ws* w, int mp, int b, const double* tau, double* Cm, int ldc,
                            int nc2) {
   const hq_device_info* dev = &w->ds->dev;
+  /* The Gram Z = U^T U stays FP64 in both precisions: a split-digit product
+   * scales each column of U by its unit diagonal entry, so the long dot
+   * products of the small entries below it would lose about 2^-47 -- enough
+   * to cost T, and with it the block reflector, orthogonality. */
   DG('T', 'N', b, b, mp, 1.0, w->U, w->ldu, w->U, w->ldu, 0.0, w->Z, w->ldz);
   CK(hq_larft_from_gram(w->st, b, w->Z, w->ldz, tau, w->T, w->ldt));
   prof_mark(w, PH_PANEL, 2.0 * mp * b * b + (double)b * b * b / 3.0);
   if (nc2 > 0 && w->mixed) {
-    /* W1 = U^T C and C -= U W2 on the tensor cores; W2 = T^T W1 in FP64. */
+    /* W1 = U^T C, W2 = T^T W1 and C -= U W2 on the tensor cores. */
     int rc = ozk_product(w, OZK_SLICES, b, nc2, mp, w->U, w->ldu, 1, Cm, ldc, 1, 0, 1.0, w->W1,
                          1, w->ldw);
     if (rc) return rc;
-    DG('T', 'N', b, nc2, b, 1.0, w->T, w->ldt, w->W1, w->ldw, 0.0, w->W2, w->ldw);
-    prof_mark(w, PH_UPDATE, (double)b * b * nc2);
+    rc = ozk_product(w, OZK_SLICES, b, nc2, b, w->T, w->ldt, 1, w->W1, w->ldw, 1, 0, 1.0, w->W2, 1,
+                     w->ldw);
+    if (rc) return rc;
     rc = ozk_product(w, OZK_SLICES, mp, nc2, b, w->U, 1, w->ldu, w->W2, w->ldw, 1, 1, -1.0, Cm, 1,
                      ldc);
     if (rc) return rc;
@@ -433,8 +440,10 @@ static int core_hqrrp_k(hq_ws* w, int m, int n, double* dA, int ldda, int* djpvt
 
     if (!last) {
       /* Pivot selection on the sketch, then one gather of A, Y and jpvt. */
+      /* Mixed: the sketch's reflector applications in FP32 (it is formed from
+       * two-digit BF16 operands and only steers pivots); norms stay FP64. */
       CK(hq_skinny_qrp(w->st, dev, mY, n - j, b, YR, w->ldy, w->V, w->ldy, w->pairs, w->npairs,
-                       w->part, w->part_elems, w->bar, w->err, spin));
+                       w->part, w->part_elems, w->bar, w->err, spin, w->mixed));
       CK(hq_permute_pairs(w->st, m, AR, ldda, n - j, w->pairs, w->npairs, 2 * b, w->tmp,
                           djpvt + j, w->label_tmp));
       CK(hq_permute_pairs(w->st, mY, YR, w->ldy, n - j, w->pairs, w->npairs, 2 * b, w->tmp, NULL,
@@ -469,8 +478,10 @@ static int core_hqrrp_k(hq_ws* w, int m, int n, double* dA, int ldda, int* djpvt
         int rc = ozk_product(w, OZK_SLICES, b, mY, mp, w->U, w->ldu, 1, GR, 1, w->ldg, 0, 1.0,
                              w->Bm, w->ldb, 1);
         if (rc) return rc;
-        DG('N', 'N', mY, b, b, 1.0, w->Bm, w->ldb, w->T, w->ldt, 0.0, w->B2, w->ldb);
-        prof_mark(w, PH_DOWNDATE, 2.0 * mY * b * b);
+        /* B2 = Bm T (mY x b x b): too few tiles for the FP64 kernel to fill the GPU. */
+        rc = ozk_product(w, OZK_SLICES, mY, b, b, w->Bm, 1, w->ldb, w->T, w->ldt, 1, 0, 1.0, w->B2,
+                         1, w->ldb);
+        if (rc) return rc;
         rc = ozk_product(w, OZK_SLICES, mp, mY, b, w->U, 1, w->ldu, w->B2, 1, w->ldb, 1, -1.0, GR,
                          w->ldg, 1);
         if (rc) return rc;

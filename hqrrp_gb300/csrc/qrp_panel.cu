@@ -428,15 +428,20 @@ int panel_grid(const hq_device_info* dev, int mp) {
 
 // DLARFT (Forward, Columnwise) from the Gram matrix Z = U^T U: for each i,
 // T[0:i, i] = -tau_i T[0:i, 0:i] Z[0:i, i] and T[i, i] = tau_i (T[0:i, i] = 0
-// when tau_i = 0).  One CTA; T is built in shared memory when it fits.
+// when tau_i = 0).  One CTA; the columns are a sequential recurrence, so each
+// step's triangular matrix-vector product is spread over the CTA with eight
+// lanes per row (short FP64 dependency chains), combined by shuffles.  T is
+// built in shared memory with an odd leading dimension (no bank conflicts
+// between the eight lanes of a row) when it fits.
 __global__ void larft_kernel(int k, const double* __restrict__ Z, int ldz,
                              const double* __restrict__ tau, double* __restrict__ T, int ldt,
                              int use_smem) {
   extern __shared__ double sT[];
   __shared__ double tmp[HQ_MAX_MY];
   double* Tm = use_smem ? sT : T;
-  const int ld = use_smem ? k : ldt;
+  const int ld = use_smem ? (k | 1) : ldt;
   const int tid = threadIdx.x, nt = blockDim.x;
+  const int g = tid & 7, rows_per_pass = nt >> 3;
   for (int e = tid; e < k * k; e += nt) Tm[(e % k) + (size_t)(e / k) * ld] = 0.0;
   __syncthreads();
   for (int i = 0; i < k; ++i) {
@@ -444,10 +449,15 @@ __global__ void larft_kernel(int k, const double* __restrict__ Z, int ldz,
     for (int r = tid; r < i; r += nt) tmp[r] = -ti * Z[r + (size_t)i * ldz];
     __syncthreads();
     if (ti != 0.0) {
-      for (int r = tid; r < i; r += nt) {
-        double s = 0.0;
-        for (int c = r; c < i; ++c) s = fma(Tm[r + (size_t)c * ld], tmp[c], s);
-        Tm[r + (size_t)i * ld] = s;
+      for (int r0 = 0; r0 < i; r0 += rows_per_pass) {
+        const int r = r0 + (tid >> 3);
+        double acc = 0.0;
+        if (r < i)
+          for (int c = r + g; c < i; c += 8) acc = fma(Tm[r + (size_t)c * ld], tmp[c], acc);
+        acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+        acc += __shfl_xor_sync(0xffffffffu, acc, 2);
+        acc += __shfl_xor_sync(0xffffffffu, acc, 4);
+        if (g == 0 && r < i) Tm[r + (size_t)i * ld] = acc;
       }
     }
     if (tid == 0) Tm[i + (size_t)i * ld] = ti;
@@ -455,7 +465,7 @@ __global__ void larft_kernel(int k, const double* __restrict__ Z, int ldz,
   }
   if (use_smem)
     for (int e = tid; e < k * k; e += nt)
-      T[(e % k) + (size_t)(e / k) * ldt] = sT[(e % k) + (size_t)(e / k) * k];
+      T[(e % k) + (size_t)(e / k) * ldt] = sT[(e % k) + (size_t)(e / k) * ld];
 }
 
 }  // namespace
@@ -519,7 +529,7 @@ extern "C" int hq_larft_from_gram(cudaStream_t stream, int k, const double* Z, i
                                   const double* tau, double* T, int ldt) {
   if (k <= 0) return 0;
   if (k > HQ_MAX_MY) return (int)cudaErrorInvalidValue;
-  const size_t smem = sizeof(double) * (size_t)k * k;
+  const size_t smem = sizeof(double) * (size_t)k * (k | 1);
   if (smem <= 160 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(larft_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);

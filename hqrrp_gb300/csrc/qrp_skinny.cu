@@ -278,16 +278,22 @@ __global__ void __launch_bounds__(NT, 1) skinny_qrp_kernel(SkArgs a) {
 // keys.  Used when a CTA's range has at most NT/2 columns and mY <= 2 * RPT;
 // otherwise the shared-memory kernel above runs.  Record layout (as 64-bit
 // integers): [0] norm key, [1] position, [2] column, then the column's entries.
+//
+// T is the arithmetic of the reflector applications (the bulk of the FP64
+// work): double for the plain path, float for the mixed path, whose sketch is
+// formed from two-digit BF16 operands (~16 significant bits) and only steers
+// pivots.  Norms, their LAWN 176 downdate and recomputation, and the
+// reflector scalars are FP64 in both.
 __device__ __forceinline__ bool better_key(long long k1, int p1, long long k2, int p2) {
   return k1 > k2 || (k1 == k2 && p1 < p2);
 }
 
-template <int RPT>
+template <int RPT, typename T>
 __global__ void __launch_bounds__(NT, 1) skinny_qrp_reg_kernel(SkArgs a) {
   constexpr int NCH = RPT / 8;  // chunks of 8 registers = 16 rows
   constexpr int NC = NT / 2;
   __shared__ __align__(16) double sv[2 * RPT];   // winner column (raw)
-  __shared__ __align__(16) double sv2[2 * RPT];  // the reflector v
+  __shared__ __align__(16) T sv2[2 * RPT];  // the reflector v
   __shared__ long long s_bk[NWARP];
   __shared__ int s_bp[NWARP], s_bc[NWARP];
   __shared__ int spos[NC], sflag[NC];
@@ -304,15 +310,15 @@ __global__ void __launch_bounds__(NT, 1) skinny_qrp_reg_kernel(SkArgs a) {
   const int c = tid >> 1;  // this pair's local column
   const bool have = c < nloc;
 
-  double x[RPT];
+  T x[RPT];
   {
     const double* src = a.Y + (size_t)(c_lo + (have ? c : 0)) * a.ldy;
     double q = 0.0;
 #pragma unroll
     for (int i = 0; i < RPT; ++i) {
       const int r = 2 * i + h;
-      x[i] = (have && r < mY) ? src[r] : 0.0;
-      q = fma(x[i], x[i], q);
+      x[i] = (have && r < mY) ? (T)src[r] : (T)0;
+      q = fma((double)x[i], (double)x[i], q);
     }
     q += __shfl_xor_sync(0xffffffffu, q, 1);
     if (have && h == 0) {
@@ -321,7 +327,7 @@ __global__ void __launch_bounds__(NT, 1) skinny_qrp_reg_kernel(SkArgs a) {
       spos[c] = c_lo + c;
     }
   }
-  for (int r = tid; r < 2 * RPT; r += NT) sv2[r] = 0.0;
+  for (int r = tid; r < 2 * RPT; r += NT) sv2[r] = (T)0;
   __syncthreads();
 
   unsigned epoch = 0;
@@ -358,7 +364,7 @@ __global__ void __launch_bounds__(NT, 1) skinny_qrp_reg_kernel(SkArgs a) {
 #pragma unroll
       for (int i = 0; i < RPT; ++i) {
         const int r = 2 * i + h;
-        if (r >= s && r < mY) rec[HDR + r] = x[i];
+        if (r >= s && r < mY) rec[HDR + r] = (double)x[i];
       }
     }
   };
@@ -435,10 +441,10 @@ __global__ void __launch_bounds__(NT, 1) skinny_qrp_reg_kernel(SkArgs a) {
       }
       __syncwarp();
       const double scale = s_scale;
-      for (int r = s + 1 + lane; r < mY; r += 32) sv2[r] = scale * sv[r];
+      for (int r = s + 1 + lane; r < mY; r += 32) sv2[r] = (T)(scale * sv[r]);
       if (lane == 0) {
-        sv2[s] = 1.0;
-        if (s > 0) sv2[s - 1] = 0.0;
+        sv2[s] = (T)1;
+        if (s > 0) sv2[s - 1] = (T)0;
       }
     }
     __syncthreads();
@@ -448,7 +454,7 @@ __global__ void __launch_bounds__(NT, 1) skinny_qrp_reg_kernel(SkArgs a) {
     const bool active = have && spos[c] > s;
     if (active) {
       const int sch = s >> 4;  // first chunk holding a row >= s
-      double w = 0.0;
+      T w = (T)0;
 #pragma unroll
       for (int ch = 0; ch < NCH; ++ch) {
         if (ch >= sch && 16 * ch < mY) {
@@ -457,8 +463,8 @@ __global__ void __launch_bounds__(NT, 1) skinny_qrp_reg_kernel(SkArgs a) {
         }
       }
       w += __shfl_xor_sync(pmask, w, 1);
-      const double g = -s_tau * w;
-      double xs_new = 0.0;
+      const T g = (T)(-s_tau) * w;
+      T xs_new = (T)0;
 #pragma unroll
       for (int ch = 0; ch < NCH; ++ch) {
         if (ch >= sch && 16 * ch < mY) {
@@ -469,7 +475,7 @@ __global__ void __launch_bounds__(NT, 1) skinny_qrp_reg_kernel(SkArgs a) {
           }
         }
       }
-      if (h == (s & 1)) srs[c] = xs_new;
+      if (h == (s & 1)) srs[c] = (double)xs_new;
     }
     __syncthreads();
     // Norm downdate, one thread per column (LAWN 176); flagged norms are
@@ -494,7 +500,7 @@ __global__ void __launch_bounds__(NT, 1) skinny_qrp_reg_kernel(SkArgs a) {
 #pragma unroll
         for (int i = 0; i < RPT; ++i) {
           const int r = 2 * i + h;
-          if (r > s) q2 = fma(x[i], x[i], q2);
+          if (r > s) q2 = fma((double)x[i], (double)x[i], q2);
         }
         q2 += __shfl_xor_sync(pmask, q2, 1);
         const double dc = (mY - s - 1 > 0) ? sqrt(q2) : 0.0;
@@ -538,7 +544,7 @@ extern "C" size_t hq_skinny_part_elems(const hq_device_info* dev, int mY) {
 extern "C" int hq_skinny_qrp(cudaStream_t stream, const hq_device_info* dev, int mY, int N,
                              int b, const double* Y, int ldy, double* V, int ldv, int* pairs,
                              int* npairs, double* part, size_t part_elems, unsigned* bar,
-                             int* err, unsigned spin_limit) {
+                             int* err, unsigned spin_limit, int fp32) {
   if (mY > HQ_MAX_MY || b > mY || b > N || b <= 0) return (int)cudaErrorInvalidValue;
   SkArgs a;
   a.mY = mY;
@@ -578,8 +584,10 @@ extern "C" int hq_skinny_qrp(cudaStream_t stream, const hq_device_info* dev, int
   void* args[] = {&a};
   const void* fn = nullptr;
   const bool reg_ok = a.nloc_max <= NT / 2 && P <= 160;  // 5 records per lane in the winner pick
-  if (reg_ok && mY <= 2 * 40) fn = (const void*)skinny_qrp_reg_kernel<40>;
-  else if (reg_ok && mY <= 2 * 72) fn = (const void*)skinny_qrp_reg_kernel<72>;
+  if (reg_ok && mY <= 2 * 40)
+    fn = fp32 ? (const void*)skinny_qrp_reg_kernel<40, float> : (const void*)skinny_qrp_reg_kernel<40, double>;
+  else if (reg_ok && mY <= 2 * 72)
+    fn = fp32 ? (const void*)skinny_qrp_reg_kernel<72, float> : (const void*)skinny_qrp_reg_kernel<72, double>;
   if (fn != nullptr) {
     e = cudaLaunchCooperativeKernel(fn, dim3(P), dim3(NT), args, 0, stream);
   } else {
