@@ -1,5 +1,6 @@
 // adjoint.cu -- small kernels of the hand-written adjoint of the truncated
-// factorization A P ~= Q_k R_k (no counterpart in the reference).
+// factorization A P ~= Q_k R_k (no counterpart in the reference), and the
+// element-wise pieces of the mixed path's unit-diagonal handling.
 //
 // For L = <W, Q_k R_k P^T> = <W, Q Q^T A> with the pivots P held fixed, Q
 // depends only on A1 = A P[:, :k] = Q R11 (a thin Householder QR), and
@@ -88,6 +89,36 @@ __global__ void rk_unpermute_kernel(int k, int n, const double* __restrict__ F, 
   }
 }
 
+// dst (rows x cols) += alpha * src.
+__global__ void add_matrix_kernel(int rows, int cols, double alpha, const double* __restrict__ src,
+                                  int lds, double* __restrict__ dst, int ldd) {
+  const long long total = (long long)rows * cols;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e % rows), j = (int)(e / rows);
+    dst[i + (long long)j * ldd] = fma(alpha, src[i + (long long)j * lds], dst[i + (long long)j * ldd]);
+  }
+}
+
+// A[i, i] = v for i < n.
+__global__ void set_diag_kernel(int n, double* __restrict__ A, int lda, double v) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    A[i + (long long)i * lda] = v;
+}
+
+// Z (b x b) += L + L^T + I where L is the strictly lower b x b top block of
+// U' (U with its unit diagonal removed): the terms of U^T U that involve the
+// unit diagonal, U^T U = U'^T U' + L + L^T + I.
+__global__ void gram_unit_fix_kernel(int b, const double* __restrict__ Up, int ldu,
+                                     double* __restrict__ Z, int ldz) {
+  const int total = b * b;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+    const int r = e % b, c = e / b;
+    const double add = r == c ? 1.0 : (r > c ? Up[r + (long long)c * ldu] : Up[c + (long long)r * ldu]);
+    Z[r + (long long)c * ldz] += add;
+  }
+}
+
 inline unsigned grid_for(long long total) {
   long long b = (total + 255) / 256;
   if (b > 8192) b = 8192;
@@ -140,6 +171,30 @@ extern "C" int hq_rk_unpermute(cudaStream_t st, int k, int n, const double* F, i
                                const int* labels, double* M, int ldm) {
   if (k <= 0 || n <= 0) return 0;
   rk_unpermute_kernel<<<grid_for((long long)k * n), 256, 0, st>>>(k, n, F, ldf, labels, M, ldm);
+  hq_count_launches(1);
+  return (int)cudaGetLastError();
+}
+
+extern "C" int hq_add_matrix(cudaStream_t st, int rows, int cols, double alpha, const double* src,
+                             int lds, double* dst, int ldd) {
+  if (rows <= 0 || cols <= 0) return 0;
+  add_matrix_kernel<<<grid_for((long long)rows * cols), 256, 0, st>>>(rows, cols, alpha, src, lds,
+                                                                      dst, ldd);
+  hq_count_launches(1);
+  return (int)cudaGetLastError();
+}
+
+extern "C" int hq_set_diag(cudaStream_t st, int n, double* A, int lda, double v) {
+  if (n <= 0) return 0;
+  set_diag_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, A, lda, v);
+  hq_count_launches(1);
+  return (int)cudaGetLastError();
+}
+
+extern "C" int hq_gram_unit_fix(cudaStream_t st, int b, const double* Up, int ldu, double* Z,
+                                int ldz) {
+  if (b <= 0) return 0;
+  gram_unit_fix_kernel<<<grid_for((long long)b * b), 256, 0, st>>>(b, Up, ldu, Z, ldz);
   hq_count_launches(1);
   return (int)cudaGetLastError();
 }

@@ -131,6 +131,12 @@ unsigned hq_spin_limit(void);
 
 /* ---- Small kernels ---- */
 int hq_fill_iota(cudaStream_t stream, int* x, int n, int base);
+/* dst += alpha * src; A[i, i] = v; Z += L + L^T + I (L: strictly lower top
+ * b x b block of U with its unit diagonal removed). */
+int hq_add_matrix(cudaStream_t st, int rows, int cols, double alpha, const double* src, int lds,
+                  double* dst, int ldd);
+int hq_set_diag(cudaStream_t st, int n, double* A, int lda, double v);
+int hq_gram_unit_fix(cudaStream_t st, int b, const double* Up, int ldu, double* Z, int ldz);
 int hq_copy_matrix(cudaStream_t stream, int rows, int cols, const double* src, int lds,
                    double* dst, int ldd);
 

@@ -317,6 +317,7 @@ static int ws_setup(hq_ws* w, int m, int n, int nb, int pp, int pw) {
     if ((t = ozk_b_bytes(mY, kmax, S)) > b) b = t;
     if ((t = hq_ozk_tile_bytes(mY, kmax, S, 0)) > a) a = t; /* B2 = Bm T */
     if ((t = ozk_b_bytes(kmax, kmax, S)) > b) b = t;
+    if ((t = ozk_b_bytes(kmax, m, S)) > b) b = t;            /* Gram U'^T U' */
     const int rows = imax(imax(m, n), mY) + 128;
     w->ozA = ws_alloc(w, a);
     w->ozB = ws_alloc(w, b);
@@ -370,28 +371,40 @@ static int ozk_product(hq_ws* w, int S, int M, int N, int K, const double* X, lo
 }
 
 /* Build T for the b reflectors in U (mp rows) and apply Q^T from the left to
- * C (mp x nc2): the dlarfb('L','T','F','C') of ...var4.c:711-740. */
+ * C (mp x nc2): the dlarfb('L','T','F','C') of ...var4.c:711-740.
+ *
+ * Mixed mode: w->U holds U' = U - [I_b; 0] (the unit diagonal removed).  A
+ * split-digit product scales each operand row by its largest entry; with the
+ * unit diagonal present that scale is 1 and the small entries below it lose
+ * ~2^-47 over long dot products.  The identity's share is exact algebra added
+ * in FP64: U^T U = U'^T U' + L + L^T + I, U^T C = U'^T C + C[0:b, :],
+ * U W2 = U' W2 + [W2; 0]. */
 static int block_reflector(hq_ws* w, int mp, int b, const double* tau, double* Cm, int ldc,
                            int nc2) {
   const hq_device_info* dev = &w->ds->dev;
-  /* The Gram Z = U^T U stays FP64 in both precisions: a split-digit product
-   * scales each column of U by its unit diagonal entry, so the long dot
-   * products of the small entries below it would lose about 2^-47 -- enough
-   * to cost T, and with it the block reflector, orthogonality. */
-  DG('T', 'N', b, b, mp, 1.0, w->U, w->ldu, w->U, w->ldu, 0.0, w->Z, w->ldz);
+  if (w->mixed) {
+    int rc = ozk_product(w, OZK_SLICES, b, b, mp, w->U, w->ldu, 1, w->U, w->ldu, 1, 0, 1.0, w->Z,
+                         1, w->ldz);
+    if (rc) return rc;
+    CK(hq_gram_unit_fix(w->st, b, w->U, w->ldu, w->Z, w->ldz));
+  } else {
+    DG('T', 'N', b, b, mp, 1.0, w->U, w->ldu, w->U, w->ldu, 0.0, w->Z, w->ldz);
+  }
   CK(hq_larft_from_gram(w->st, b, w->Z, w->ldz, tau, w->T, w->ldt));
-  prof_mark(w, PH_PANEL, 2.0 * mp * b * b + (double)b * b * b / 3.0);
+  prof_mark(w, PH_PANEL, (w->mixed ? 0.0 : 2.0 * mp * b * b) + (double)b * b * b / 3.0);
   if (nc2 > 0 && w->mixed) {
     /* W1 = U^T C, W2 = T^T W1 and C -= U W2 on the tensor cores. */
     int rc = ozk_product(w, OZK_SLICES, b, nc2, mp, w->U, w->ldu, 1, Cm, ldc, 1, 0, 1.0, w->W1,
                          1, w->ldw);
     if (rc) return rc;
+    CK(hq_add_matrix(w->st, b, nc2, 1.0, Cm, ldc, w->W1, w->ldw));
     rc = ozk_product(w, OZK_SLICES, b, nc2, b, w->T, w->ldt, 1, w->W1, w->ldw, 1, 0, 1.0, w->W2, 1,
                      w->ldw);
     if (rc) return rc;
     rc = ozk_product(w, OZK_SLICES, mp, nc2, b, w->U, 1, w->ldu, w->W2, w->ldw, 1, 1, -1.0, Cm, 1,
                      ldc);
     if (rc) return rc;
+    CK(hq_add_matrix(w->st, b, nc2, -1.0, w->W2, w->ldw, Cm, ldc));
   } else if (nc2 > 0) {
     DG('T', 'N', b, nc2, mp, 1.0, w->U, w->ldu, Cm, ldc, 0.0, w->W1, w->ldw);
     DG('T', 'N', b, nc2, b, 1.0, w->T, w->ldt, w->W1, w->ldw, 0.0, w->W2, w->ldw);
@@ -456,6 +469,7 @@ static int core_hqrrp_k(hq_ws* w, int m, int n, double* dA, int ldda, int* djpvt
     /* Panel QR (pivoted within its b columns), U, tau. */
     CK(hq_panel_qrp(w->st, dev, mp, b, panel_piv, ABR, ldda, dtau + j, w->U, w->ldu, w->perm,
                     w->part, w->part_elems, w->rowbuf, w->bar + 1, w->err, spin));
+    if (w->mixed) CK(hq_set_diag(w->st, b, w->U, w->ldu, 0.0)); /* U' for the digit products */
     /* The panel's swaps on the rows above it and on the labels. */
     CK(hq_permute_cols(w->st, j, AR, ldda, b, w->perm, w->tmp, djpvt + j, w->label_tmp));
     {
@@ -475,9 +489,12 @@ static int core_hqrrp_k(hq_ws* w, int m, int n, double* dA, int ldda, int* djpvt
       if (w->mixed) {
         /* B^T = U^T G_R^T; G_R^T -= U B2^T; Y2^T -= R12^T G1^T (transposed so the
          * long dimension is the 128-row tile side). */
+        /* U holds U' (unit diagonal removed): Bm = G_R U' + G_R[:, 0:b] and
+         * G_R -= B2 U'^T + [B2, 0]. */
         int rc = ozk_product(w, OZK_SLICES, b, mY, mp, w->U, w->ldu, 1, GR, 1, w->ldg, 0, 1.0,
                              w->Bm, w->ldb, 1);
         if (rc) return rc;
+        CK(hq_add_matrix(w->st, mY, b, 1.0, GR, w->ldg, w->Bm, w->ldb));
         /* B2 = Bm T (mY x b x b): too few tiles for the FP64 kernel to fill the GPU. */
         rc = ozk_product(w, OZK_SLICES, mY, b, b, w->Bm, 1, w->ldb, w->T, w->ldt, 1, 0, 1.0, w->B2,
                          1, w->ldb);
@@ -485,6 +502,7 @@ static int core_hqrrp_k(hq_ws* w, int m, int n, double* dA, int ldda, int* djpvt
         rc = ozk_product(w, OZK_SLICES, mp, mY, b, w->U, 1, w->ldu, w->B2, 1, w->ldb, 1, -1.0, GR,
                          w->ldg, 1);
         if (rc) return rc;
+        CK(hq_add_matrix(w->st, mY, b, -1.0, w->B2, w->ldb, GR, w->ldg));
         rc = ozk_product(w, OZK_SLICES, nc2, mY, b, ABR + (size_t)b * ldda, ldda, 1, GR, 1, w->ldg,
                          1, -1.0, YR + (size_t)b * w->ldy, w->ldy, 1);
         if (rc) return rc;
@@ -719,6 +737,7 @@ static int core_dgeqp4(hq_ws* w, int m, int n, double* dA, int ldda, int* hjp, i
     double* ABR = dA + j + (size_t)j * ldda;
     CK(hq_panel_qrp(w->st, dev, mp, b, 0, ABR, ldda, dtau + j, w->U, w->ldu, w->perm, w->part,
                     w->part_elems, w->rowbuf, w->bar + 1, w->err, spin));
+    if (w->mixed) CK(hq_set_diag(w->st, b, w->U, w->ldu, 0.0)); /* U' for the digit products */
     int rc = block_reflector(w, mp, b, dtau + j, ABR + (size_t)b * ldda, ldda, n - j - b);
     if (rc) return rc;
   }
