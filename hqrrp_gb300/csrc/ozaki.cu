@@ -90,10 +90,14 @@ __device__ __forceinline__ uint32_t digit_f32(uint32_t u) {
   return __float_as_uint(__fsub_rn(__uint_as_float(0x4B000000u | u), 8388736.0f));
 }
 
-// The same digit times 2^(-8s) for slice s (exact: a power-of-two scale of a
-// small integer), so that products carry their level's weight.
+// The same digit times 2^(-8s) for slice s, so that products carry their
+// level's weight: the FP32 pattern with exponent 23 - 8s and mantissa u is
+// 2^(23-8s) + u 2^(-8s) exactly, and subtracting 2^(23-8s) + 128 2^(-8s)
+// (exact in FP32) leaves (u - 128) 2^(-8s) in one add.
 __device__ __forceinline__ uint32_t digit_scaled(uint32_t u, int s) {
-  return __float_as_uint(__fmul_rn(__uint_as_float(digit_f32(u)), __int_as_float((127 - 8 * s) << 23)));
+  const float base = __uint_as_float(((uint32_t)(150 - 8 * s) << 23) | u);
+  const float off = __uint_as_float(((uint32_t)(150 - 8 * s) << 23) | 128u);
+  return __float_as_uint(__fsub_rn(base, off));
 }
 
 // Rows r < R of X (element (r, k) at X[r*rs + k*ks], k < K) -> S digit tiles.
@@ -189,12 +193,25 @@ __global__ void __launch_bounds__(512) ozk_split_row_kernel(
     const double* xr = X + (live ? (long long)r * rs : 0);
     double v[CPT][8];
     long long mb = 0;
+    // Contiguous, 16-byte aligned rows are read with 16-byte loads.
+    const bool vec = ks == 1 && ((reinterpret_cast<uintptr_t>(xr) & 15) == 0);
 #pragma unroll
     for (int i = 0; i < CPT; ++i) {
       const int k0 = (tid + i * NTH) * 8;
+      if (vec && live && k0 + 8 <= K) {
+        const double2* p2 = reinterpret_cast<const double2*>(xr + k0);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const double2 d = p2[j];
+          v[i][2 * j] = d.x;
+          v[i][2 * j + 1] = d.y;
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) v[i][j] = (live && k0 + j < K) ? xr[(long long)(k0 + j) * ks] : 0.0;
+      }
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
-        v[i][j] = (live && k0 + j < K) ? xr[(long long)(k0 + j) * ks] : 0.0;
         const long long bb = __double_as_longlong(v[i][j]) & 0x7FFFFFFFFFFFFFFFLL;
         mb = bb > mb ? bb : mb;
       }
