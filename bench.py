@@ -47,6 +47,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "dgeqp4 TFLOP/s at n=16384, mixed vs plain FP64 at equal residual; bwd ms"
+# DRAM bytes per algorithmic flop of the dominant kernels, from ncu captures at
+# m = n = 6144 (committed summaries under profiles/): the split-BF16 products
+# (W1 and the rank-b update) and the FP64 update GEMMs (W1, C -= U W2).
+TENSOR_BYTES_PER_FLOP = (550.2e6 + 556.1e6) / (2 * 2.649e11)
+FP64_UPDATE_BYTES_PER_FLOP = (314.4e6 + 546.3e6) / (2 * 9.462e9)
 
 
 def flops_qr(m, n):
@@ -339,15 +344,17 @@ def run_arm(hq, precision, At0, At, jp, iota, tau, nb, pp, sigma, args, device, 
     # One more (untimed) factorization under the phase profiler.
     hq.profile_enable(True)
     hq.profile_read()
+    hq.profile_counts()
     step()
     torch.cuda.synchronize()
     prof = hq.profile_read()
+    counts = hq.profile_counts()
     hq.profile_enable(False)
     return {"ms_per_step": ms / args.steps, "launches": launches, "clocks": clocks,
             "quality": {"residual_est": res, "orthogonality_est": orth,
                         "rkk_over_sigma_min": float(ratio.min()),
                         "rkk_over_sigma_max": float(ratio.max())},
-            "ratio": ratio, "prof": prof}
+            "ratio": ratio, "prof": prof, "counts": counts}
 
 
 def phase_table(prof):
@@ -516,7 +523,7 @@ def run_batched(hq, args, device, dist, rank, world, local):
                                  % (8 * offs[-1] * world / 1e9)},
                 "matrices_per_s": len(shapes_all) / (ms * 1e-3),
                 "quality": {"residual_max_sample": worst},
-                "roofline": {"bound": "fp64", "achieved": value,
+                "roofline": {"bound": "tensor", "pipe": "fp64", "achieved": value,
                              "peak": fp64_peak_tflops(device), "unit": "TFLOP/s",
                              "kernel": "qrp_batched_kernel (whole step)",
                              "peak_source": "cuBLAS DGEMM 8192^3 measured in this run",
@@ -617,24 +624,37 @@ def main():
     # profile: mixed -> ozk_gemm_kernel (BF16 tensor work), plain -> dgemm_tile.
     if head == "mixed":
         t_ms, t_fl = H["prof"]["tensor"]
+        n_t = max(1, H["counts"].get("tensor", 0))
         peak = peaks.get("bf16_tflops_sustained") or 1700.0
         achieved = t_fl / (t_ms * 1e-3) / 1e12 if t_ms > 0 else None
-        roofline = {"bound": "tensor", "pipe": "bf16 tcgen05", "kernel": "ozk_gemm_kernel "
-                    "(split-BF16 digit products of the block update and sketch downdate)",
+        roofline = {"bound": "tensor", "pipe": "bf16 tcgen05",
+                    "kernel": "ozk_gemm_kernel + ozk_gemm_short_kernel (split-BF16 digit "
+                              "products of the block update, Gram, T^T W1 and sketch downdate)",
                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                     "frac": achieved / peak if achieved else None,
                     "peak_source": "bf16_tflops_sustained of measured (MEASURED_PEAKS.json)"
                     if peaks.get("bf16_tflops_sustained") else "fallback 1.7 PFLOP/s sustained",
-                    "traffic": None}
+                    "launches": n_t, "flops_per_launch": t_fl / n_t,
+                    # DRAM bytes per BF16 flop of the two large products of a block,
+                    # ncu at 6144^2 (W1 550.2 MB, C -= U'W2 556.1 MB per 2.649e11
+                    # flops each), times this run's flops per launch.
+                    "traffic": TENSOR_BYTES_PER_FLOP * t_fl / n_t,
+                    "traffic_source": "ncu dram__bytes_read+write at 6144^2 scaled by flops "
+                                      "per launch"}
     else:
         u_ms, u_fl = H["prof"]["update"]
         peak = fp64_peak_tflops(device)
         achieved = u_fl / (u_ms * 1e-3) / 1e12 if u_ms > 0 else None
+        n_u = 3 * max(1, H["counts"].get("update", 0))  # W1, W2, U3 per block
         roofline = {"bound": "tensor", "pipe": "fp64", "kernel": "dgemm_tile (trailing dlarfb update)",
                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                     "frac": achieved / peak if achieved else None,
                     "peak_source": "cuBLAS DGEMM 8192^3 measured in this run (MEASURED_PEAKS.json "
-                                   "has no FP64 figure)", "traffic": None}
+                                   "has no FP64 figure)",
+                    "launches": n_u, "flops_per_launch": u_fl / n_u,
+                    "traffic": FP64_UPDATE_BYTES_PER_FLOP * u_fl / n_u,
+                    "traffic_source": "ncu dram__bytes_read+write at 6144^2 scaled by flops "
+                                      "per launch"}
     roofline["phases_ms"], roofline["phases_tflops"] = phase_table(H["prof"])
 
     # End to end through the reference-facing C entry point, host buffers.

@@ -103,6 +103,8 @@ def load():
               "hqrrp_gb300_apply_q_device",
               "hqrrp_gb300_form_q_device", "hqrrp_gb300_hqrrp_adjoint_device"):
         getattr(L, f).restype = C.c_int
+    L.hqrrp_gb300_profile_counts.argtypes = [_ip, C.c_int]
+    L.hqrrp_gb300_profile_counts.restype = C.c_int
     L.hqrrp_gb300_last_error.argtypes = []
     L.hqrrp_gb300_last_error.restype = C.c_char_p
     _lib = L
@@ -146,6 +148,13 @@ def profile_read():
     fl = np.zeros(16)
     n = load().hqrrp_gb300_profile_read(ms.ctypes.data_as(_dp), fl.ctypes.data_as(_dp), 16)
     return {PHASES[i]: (float(ms[i]), float(fl[i])) for i in range(n)}
+
+
+def profile_counts():
+    """{phase: intervals recorded} since the last call; resets."""
+    c = np.zeros(16, dtype=np.int32)
+    n = load().hqrrp_gb300_profile_counts(c.ctypes.data_as(_ip), 16)
+    return {PHASES[i]: int(c[i]) for i in range(n)}
 
 
 def launch_count():

@@ -59,6 +59,7 @@ enum { PH_SKETCH = 0, PH_SELECT, PH_PANEL, PH_UPDATE, PH_DOWNDATE, PH_OTHER, PH_
 #define PROF_MAXEV 8192
 static int g_prof_on = 0;
 static double g_prof_ms[PH_COUNT], g_prof_flops[PH_COUNT];
+static int g_prof_n[PH_COUNT];
 static cudaEvent_t g_prof_ev[PROF_MAXEV];
 static int g_prof_ev_ready = 0;
 
@@ -204,6 +205,7 @@ static void prof_finish(hq_ws* w) {
         p->ph[i] >= 0 && p->ph[i] < PH_COUNT) {
       g_prof_ms[p->ph[i]] += ms;
       g_prof_flops[p->ph[i]] += p->fl[i];
+      g_prof_n[p->ph[i]] += 1;
     }
   }
   free(p);
@@ -219,6 +221,12 @@ HQ_API int hqrrp_gb300_profile_read(double* ms, double* flops, int n) {
   }
   memset(g_prof_ms, 0, sizeof g_prof_ms);
   memset(g_prof_flops, 0, sizeof g_prof_flops);
+  return PH_COUNT;
+}
+
+HQ_API int hqrrp_gb300_profile_counts(int* counts, int n) {
+  for (int i = 0; i < PH_COUNT && i < n; ++i) counts[i] = g_prof_n[i];
+  memset(g_prof_n, 0, sizeof g_prof_n);
   return PH_COUNT;
 }
 

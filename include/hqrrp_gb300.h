@@ -181,6 +181,9 @@ int hqrrp_gb300_hqrrp_adjoint_device(int m, int n, int k, const double* dA, int 
  * number of phases. */
 void hqrrp_gb300_profile_enable(int on);
 int hqrrp_gb300_profile_read(double* ms, double* flops, int n);
+/* Intervals recorded per phase since the last call (for the tensor phase:
+ * one per digit-product launch); resets them. */
+int hqrrp_gb300_profile_counts(int* counts, int n);
 
 /* Number of kernels this library has launched in this process. */
 unsigned long long hqrrp_gb300_launch_count(void);
