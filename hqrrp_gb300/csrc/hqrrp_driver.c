@@ -171,6 +171,10 @@ typedef struct {
   int mixed;      /* split-BF16 tensor-core block updates */
   void *ozA, *ozB; /* digit tiles of the two operands of a mixed product */
   int *ozea, *ozeb;
+  /* Side stream (high priority) for the one-SM T factor, overlapped with
+   * W1 = U^T C on st; created on first use, ordered by the two events. */
+  cudaStream_t side;
+  cudaEvent_t ev_gram, ev_t;
 } hq_ws;
 
 /* Close the interval since the previous mark and charge it to `phase`. */
@@ -247,7 +251,18 @@ static void* ws_alloc(hq_ws* w, size_t bytes) {
 }
 
 static void ws_release(hq_ws* w) {
+  if (w->side) {
+    /* Nothing may be freed while the side stream could still use it. */
+    cudaEventRecord(w->ev_t, w->side);
+    cudaStreamWaitEvent(w->st, w->ev_t, 0);
+  }
   for (int i = 0; i < w->nptr; ++i) cudaFreeAsync(w->ptrs[i], w->st);
+  if (w->side) {
+    cudaStreamDestroy(w->side);
+    cudaEventDestroy(w->ev_gram);
+    cudaEventDestroy(w->ev_t);
+    w->side = NULL;
+  }
   w->nptr = 0;
   if (w->prof) { /* an error path skipped ws_check */
     free(w->prof);
@@ -378,6 +393,16 @@ static int ozk_product(hq_ws* w, int S, int M, int N, int K, const double* X, lo
   return HQ_OK;
 }
 
+static int side_stream(hq_ws* w) {
+  if (w->side) return HQ_OK;
+  int lo = 0, hi = 0;
+  CK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+  CK(cudaEventCreateWithFlags(&w->ev_gram, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&w->ev_t, cudaEventDisableTiming));
+  CK(cudaStreamCreateWithPriority(&w->side, cudaStreamNonBlocking, hi));
+  return HQ_OK;
+}
+
 /* Build T for the b reflectors in U (mp rows) and apply Q^T from the left to
  * C (mp x nc2): the dlarfb('L','T','F','C') of ...var4.c:711-740.
  *
@@ -398,14 +423,22 @@ static int block_reflector(hq_ws* w, int mp, int b, const double* tau, double* C
   } else {
     DG('T', 'N', b, b, mp, 1.0, w->U, w->ldu, w->U, w->ldu, 0.0, w->Z, w->ldz);
   }
-  CK(hq_larft_from_gram(w->st, b, w->Z, w->ldz, tau, w->T, w->ldt));
-  prof_mark(w, PH_PANEL, (w->mixed ? 0.0 : 2.0 * mp * b * b) + (double)b * b * b / 3.0);
+  /* T (one SM, a sequential recurrence) on the side stream, overlapped with
+   * W1 = U^T C, which does not need it; st waits for T before W2. */
+  int rs = side_stream(w);
+  if (rs) return rs;
+  CK(cudaEventRecord(w->ev_gram, w->st));
+  CK(cudaStreamWaitEvent(w->side, w->ev_gram, 0));
+  CK(hq_larft_from_gram(w->side, b, w->Z, w->ldz, tau, w->T, w->ldt));
+  CK(cudaEventRecord(w->ev_t, w->side));
+  prof_mark(w, PH_PANEL, w->mixed ? 0.0 : 2.0 * mp * b * b);
   if (nc2 > 0 && w->mixed) {
     /* W1 = U^T C, W2 = T^T W1 and C -= U W2 on the tensor cores. */
     int rc = ozk_product(w, OZK_SLICES, b, nc2, mp, w->U, w->ldu, 1, Cm, ldc, 1, 0, 1.0, w->W1,
                          1, w->ldw);
     if (rc) return rc;
     CK(hq_add_matrix(w->st, b, nc2, 1.0, Cm, ldc, w->W1, w->ldw));
+    CK(cudaStreamWaitEvent(w->st, w->ev_t, 0));
     rc = ozk_product(w, OZK_SLICES, b, nc2, b, w->T, w->ldt, 1, w->W1, w->ldw, 1, 0, 1.0, w->W2, 1,
                      w->ldw);
     if (rc) return rc;
@@ -415,10 +448,13 @@ static int block_reflector(hq_ws* w, int mp, int b, const double* tau, double* C
     CK(hq_add_matrix(w->st, b, nc2, -1.0, w->W2, w->ldw, Cm, ldc));
   } else if (nc2 > 0) {
     DG('T', 'N', b, nc2, mp, 1.0, w->U, w->ldu, Cm, ldc, 0.0, w->W1, w->ldw);
+    CK(cudaStreamWaitEvent(w->st, w->ev_t, 0));
     DG('T', 'N', b, nc2, b, 1.0, w->T, w->ldt, w->W1, w->ldw, 0.0, w->W2, w->ldw);
     DG('N', 'N', mp, nc2, b, -1.0, w->U, w->ldu, w->W2, w->ldw, 1.0, Cm, ldc);
     prof_mark(w, PH_UPDATE, 4.0 * mp * b * nc2 + (double)b * b * nc2);
   }
+  /* T is read after this call (the sketch downdate, the next block). */
+  CK(cudaStreamWaitEvent(w->st, w->ev_t, 0));
   return HQ_OK;
 }
 
