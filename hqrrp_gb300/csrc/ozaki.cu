@@ -23,11 +23,13 @@
 // result is recombined in FP64.  With S = 7 the product is accurate to about
 // 2^-52 relative to |A| |B| row/column-wise.
 //
-// Layout: operands are pre-split by ozk_split_kernel into K-major BF16 tiles
-// already in the 64-byte-swizzled shared-memory order the MMA reads (rows of
-// 32 K-elements = 64 B, 8-row atoms of 512 B), grouped so that the S digit
-// tiles of one (row tile, K block) are contiguous: each pipeline stage is two
-// cp.async.bulk copies.  M tile 128 rows, N tile 64, K block 32.
+// Layout: the split writes each operand as S plain K-major BF16 digit
+// matrices D[s][row][k] (rows padded to the tile height, K to 32).  The GEMM
+// kernels read them with tensor-map TMA loads (cp.async.bulk.tensor.3d): one
+// load per operand per pipeline stage brings a box of 32 K x tile rows x S
+// digits into shared memory, swizzled by the copy engine into the 64-byte
+// pattern the MMA descriptors name (rows of 64 B, 8-row atoms of 512 B).
+// M tile 128 rows, N tile 80, K block 32.
 //
 // The GEMM kernel is warp-specialised: warp 4 issues the bulk copies into a
 // 3-stage (2 for seven digits) ring, one thread of warp 5 issues tcgen05.mma (cta_group::1,
@@ -35,7 +37,8 @@
 // 32 lanes each) and write the output.  Every wait is bounded; on expiry the
 // kernel records an error, waits (bounded) for its in-flight copies and MMAs,
 // frees its TMEM and returns.
-#include <cuda_bf16.h>
+#include <cuda.h>
+#include <cudaTypedefs.h>
 
 #include "hq_common.cuh"
 
@@ -82,14 +85,6 @@ __device__ __forceinline__ long long fixed_point(double x, int shift_base) {
   return bits < 0 ? -V : V;
 }
 
-// BF16 bit pattern (in the high half of the result) of the digit u - 128 for
-// an integer 0 <= u <= 256: 2^23 + u is exact in FP32, subtracting 2^23 + 128
-// leaves u - 128 exactly, and an integer of at most 8 significant bits has
-// zeros in the low 16 bits of its FP32 pattern.
-__device__ __forceinline__ uint32_t digit_f32(uint32_t u) {
-  return __float_as_uint(__fsub_rn(__uint_as_float(0x4B000000u | u), 8388736.0f));
-}
-
 // The same digit times 2^(-8s) for slice s, so that products carry their
 // level's weight: the FP32 pattern with exponent 23 - 8s and mantissa u is
 // 2^(23-8s) + u 2^(-8s) exactly, and subtracting 2^(23-8s) + 128 2^(-8s)
@@ -115,7 +110,8 @@ __global__ void ozk_split_kernel(const double* __restrict__ X, long long rs, lon
   const int lane = threadIdx.x & 31;
   const int warps = blockDim.x >> 5;
   const int nchunk = KB * (TK / 8);
-  const long long tile_bytes = (long long)TR * TK * 2;
+  const long long kp = (long long)KB * TK;
+  const long long slice_bytes = (long long)rows_total * kp * 2;
   for (int r = blockIdx.x * warps + (threadIdx.x >> 5); r < rows_total;
        r += gridDim.x * warps) {
     const bool live = r < R;
@@ -135,7 +131,6 @@ __global__ void ozk_split_kernel(const double* __restrict__ X, long long rs, lon
     const int bexp = (int)(mb >> 52);
     const int e = bexp == 0 ? 0 : bexp - 1022;
     if (lane == 0) exps[r] = e;
-    const int rt = r / TR, rr = r % TR;
     const int shift_base = 8 * S - 1076 - e;
     for (int ch = lane; ch < nchunk; ch += 32) {
       const int k0 = ch * 8;
@@ -146,9 +141,7 @@ __global__ void ozk_split_kernel(const double* __restrict__ X, long long rs, lon
             (live && k0 + j < K) ? fixed_point(xr[(long long)(k0 + j) * ks], shift_base) : 0;
         W[j] = (unsigned long long)V + BIAS;
       }
-      const int kb = k0 / TK, c = (k0 % TK) >> 3;
-      uint8_t* base = tiles + ((long long)(rt * KB + kb) * S) * tile_bytes + rr * 64 +
-                      ((c ^ ((rr >> 1) & 3)) << 4);
+      uint8_t* base = tiles + ((long long)r * kp + k0) * 2;
 #pragma unroll
       for (int s = 0; s < S; ++s) {
         // Slice s holds digit position p = S-1-s (slice 0 the most significant).
@@ -166,7 +159,7 @@ __global__ void ozk_split_kernel(const double* __restrict__ X, long long rs, lon
           }
           w[j >> 1] = __byte_perm(digit_scaled(u0, s), digit_scaled(u1, s), 0x7632);
         }
-        *reinterpret_cast<uint4*>(base + (long long)s * tile_bytes) =
+        *reinterpret_cast<uint4*>(base + (long long)s * slice_bytes) =
             make_uint4(w[0], w[1], w[2], w[3]);
       }
     }
@@ -187,7 +180,8 @@ __global__ void __launch_bounds__(512) ozk_split_row_kernel(
   __shared__ long long s_max[NTH / 32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nchunk = KB * (TK / 8);
-  const long long tile_bytes = (long long)TR * TK * 2;
+  const long long kp = (long long)KB * TK;
+  const long long slice_bytes = (long long)rows_total * kp * 2;
   for (int r = blockIdx.x; r < rows_total; r += gridDim.x) {
     const bool live = r < R;
     const double* xr = X + (live ? (long long)r * rs : 0);
@@ -229,7 +223,6 @@ __global__ void __launch_bounds__(512) ozk_split_row_kernel(
     const int bexp = (int)(mb >> 52);
     const int e = bexp == 0 ? 0 : bexp - 1022;
     if (tid == 0) exps[r] = e;
-    const int rt = r / TR, rr = r % TR;
     const int shift_base = 8 * S - 1076 - e;
 #pragma unroll
     for (int i = 0; i < CPT; ++i) {
@@ -239,9 +232,7 @@ __global__ void __launch_bounds__(512) ozk_split_row_kernel(
 #pragma unroll
       for (int j = 0; j < 8; ++j) W[j] = (unsigned long long)fixed_point(v[i][j], shift_base) + BIAS;
       const int k0 = ch * 8;
-      const int kb = k0 / TK, c = (k0 % TK) >> 3;
-      uint8_t* base = tiles + ((long long)(rt * KB + kb) * S) * tile_bytes + rr * 64 +
-                      ((c ^ ((rr >> 1) & 3)) << 4);
+      uint8_t* base = tiles + ((long long)r * kp + k0) * 2;
 #pragma unroll
       for (int s = 0; s < S; ++s) {
         const int p = S - 1 - s;
@@ -258,7 +249,7 @@ __global__ void __launch_bounds__(512) ozk_split_row_kernel(
           }
           w[j >> 1] = __byte_perm(digit_scaled(u0, s), digit_scaled(u1, s), 0x7632);
         }
-        *reinterpret_cast<uint4*>(base + (long long)s * tile_bytes) =
+        *reinterpret_cast<uint4*>(base + (long long)s * slice_bytes) =
             make_uint4(w[0], w[1], w[2], w[3]);
       }
     }
@@ -315,12 +306,14 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* b, unsigned bytes) {
                : "memory");
 }
 
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes,
-                                         uint64_t* bar) {
+// One box of a 3-D tensor map (k, row, digit) into shared memory, completing
+// on the mbarrier; x = k must be a multiple of 8 (16 bytes of BF16).
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z,
+                                            uint64_t* bar) {
   asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-          smem_u32(dst)),
-      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
       : "memory");
 }
 
@@ -459,7 +452,9 @@ __device__ __forceinline__ void issue_block(uint32_t tb, uint64_t da0, uint64_t 
   }
 }
 
-__global__ void __launch_bounds__(NT, 1) ozk_gemm_kernel(OzkArgs a) {
+__global__ void __launch_bounds__(NT, 1) ozk_gemm_kernel(OzkArgs a,
+                                                        const __grid_constant__ CUtensorMap tmA,
+                                                        const __grid_constant__ CUtensorMap tmB) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   __shared__ __align__(8) uint64_t full_bar[MAX_STAGES], empty_bar[MAX_STAGES];
   __shared__ __align__(8) uint64_t drain_full, drain_empty, done_bar;
@@ -507,8 +502,6 @@ __global__ void __launch_bounds__(NT, 1) ozk_gemm_kernel(OzkArgs a) {
   if (warp == PRODUCER_WARP) {
     // Producer: one elected lane streams the digit tiles through the ring.
     if (lane == 0) {
-      const uint8_t* Ab = a.A + ((long long)mt * a.KB) * a_stage;
-      const uint8_t* Bb = a.B + ((long long)nt * a.KB) * b_stage;
       for (int i = 0; i < nkb; ++i) {
         const int st = i % STAGES;
         if (!mbar_wait(&empty_bar[st], ((i / STAGES) & 1) ^ 1, lim, &s_abort)) {
@@ -516,8 +509,9 @@ __global__ void __launch_bounds__(NT, 1) ozk_gemm_kernel(OzkArgs a) {
           break;
         }
         mbar_expect_tx(&full_bar[st], (unsigned)(a_stage + b_stage));
-        bulk_g2s(sA + st * a_stage, Ab + (long long)(kb0 + i) * a_stage, a_stage, &full_bar[st]);
-        bulk_g2s(sB + st * b_stage, Bb + (long long)(kb0 + i) * b_stage, b_stage, &full_bar[st]);
+        const int k0 = (kb0 + i) * TK;
+        tma_load_3d(sA + st * a_stage, &tmA, k0, mt * TM, 0, &full_bar[st]);
+        tma_load_3d(sB + st * b_stage, &tmB, k0, nt * TN, 0, &full_bar[st]);
         ++copies_issued;
       }
     }
@@ -614,7 +608,8 @@ __global__ void __launch_bounds__(NT, 1) ozk_gemm_kernel(OzkArgs a) {
 // the TMEM back, then do the FP64 output (the part bound by the FP64 pipe and
 // by C's memory traffic) while the MMAs of the next tile run.  Mode 1
 // (C += sign * A B^T) or 0 (C = sign * A B^T), no grid.z split.
-__global__ void __launch_bounds__(NT, 1) ozk_gemm_short_kernel(OzkArgs a) {
+__global__ void __launch_bounds__(NT, 1) ozk_gemm_short_kernel(
+    OzkArgs a, const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   __shared__ __align__(8) uint64_t full_bar[MAX_STAGES], empty_bar[MAX_STAGES];
   __shared__ __align__(8) uint64_t tfull, tempty, done_bar;
@@ -662,8 +657,6 @@ __global__ void __launch_bounds__(NT, 1) ozk_gemm_short_kernel(OzkArgs a) {
       int i = 0;  // stage counter across tiles
       for (int t = blockIdx.x; t < ntiles && !s_abort; t += gridDim.x) {
         const int mt = t / NTL, nt = t % NTL;
-        const uint8_t* Ab = a.A + ((long long)mt * a.KB) * a_stage;
-        const uint8_t* Bb = a.B + ((long long)nt * a.KB) * b_stage;
         for (int kb = 0; kb < nkb; ++kb, ++i) {
           const int st = i % STAGES;
           if (!mbar_wait(&empty_bar[st], ((i / STAGES) & 1) ^ 1, lim, &s_abort)) {
@@ -671,8 +664,8 @@ __global__ void __launch_bounds__(NT, 1) ozk_gemm_short_kernel(OzkArgs a) {
             break;
           }
           mbar_expect_tx(&full_bar[st], (unsigned)(a_stage + b_stage));
-          bulk_g2s(sA + st * a_stage, Ab + (long long)kb * a_stage, a_stage, &full_bar[st]);
-          bulk_g2s(sB + st * b_stage, Bb + (long long)kb * b_stage, b_stage, &full_bar[st]);
+          tma_load_3d(sA + st * a_stage, &tmA, kb * TK, mt * TM, 0, &full_bar[st]);
+          tma_load_3d(sB + st * b_stage, &tmB, kb * TK, nt * TN, 0, &full_bar[st]);
           ++copies_issued;
         }
       }
@@ -810,6 +803,33 @@ extern "C" int hq_ozk_split(cudaStream_t stream, const double* X, long long rs, 
   return (int)cudaGetLastError();
 }
 
+// Tensor map of a split operand: D[s][row][k], BF16, dims (k, row, digit) =
+// (kp, rows_p, S); box 32 x tile_rows x S, 64-byte swizzle.
+static int make_digit_map(CUtensorMap* map, const void* tiles, int rows, int K, int S,
+                          int tile_rows) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  if (encode == nullptr) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
+                                                     cudaEnableDefault, &q);
+    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || fn == nullptr)
+      return (int)cudaErrorNotSupported;
+    encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }
+  const cuuint64_t rp = (cuuint64_t)((rows + tile_rows - 1) / tile_rows) * tile_rows;
+  const cuuint64_t kp = (cuuint64_t)((K + TK - 1) / TK) * TK;
+  const cuuint64_t dims[3] = {kp, rp, (cuuint64_t)S};
+  const cuuint64_t strides[2] = {kp * 2, rp * kp * 2};  // bytes, dims 1 and 2
+  const cuuint32_t box[3] = {(cuuint32_t)TK, (cuuint32_t)tile_rows, (cuuint32_t)S};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(tiles), dims,
+                      strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                      CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? 0 : (int)cudaErrorInvalidValue;
+}
+
 extern "C" int hq_ozk_gemm(cudaStream_t stream, const hq_device_info* dev, int M, int N, int K,
                            int S, const void* Atiles, const int* ea, const void* Btiles,
                            const int* eb, int mode, double sign, double* C, long long crs,
@@ -863,10 +883,14 @@ extern "C" int hq_ozk_gemm(cudaStream_t stream, const hq_device_info* dev, int M
   }
   if (smem > dev->smem_optin) return (int)cudaErrorInvalidValue;
   a.stages = stages;
+  CUtensorMap tmA, tmB;
+  int rc = make_digit_map(&tmA, Atiles, M, K, S, TM);
+  if (rc == 0) rc = make_digit_map(&tmB, Btiles, N, K, S, TN);
+  if (rc) return rc;
   cudaError_t e =
       cudaFuncSetAttribute(ozk_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return (int)e;
-  ozk_gemm_kernel<<<dim3(MT, NTL, Z), NT, smem, stream>>>(a);
+  ozk_gemm_kernel<<<dim3(MT, NTL, Z), NT, smem, stream>>>(a, tmA, tmB);
   hq_count_launches(1);
   if (Z > 1) {
     long long total = (long long)M * N;
@@ -914,12 +938,16 @@ extern "C" int hq_ozk_gemm_short(cudaStream_t stream, const hq_device_info* dev,
   const size_t smem = (size_t)stages * per_stage + 1024;
   if (smem > dev->smem_optin) return (int)cudaErrorInvalidValue;
   a.stages = stages;
+  CUtensorMap tmA, tmB;
+  int rc = make_digit_map(&tmA, Atiles, M, K, S, TM);
+  if (rc == 0) rc = make_digit_map(&tmB, Btiles, N, K, S, TNV);
+  if (rc) return rc;
   cudaError_t e = cudaFuncSetAttribute(ozk_gemm_short_kernel,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return (int)e;
   const long long tiles = (long long)((M + TM - 1) / TM) * ((N + TNV - 1) / TNV);
   const int grid = (int)(tiles < dev->num_sms ? tiles : dev->num_sms);
-  ozk_gemm_short_kernel<<<grid, NT, smem, stream>>>(a);
+  ozk_gemm_short_kernel<<<grid, NT, smem, stream>>>(a, tmA, tmB);
   hq_count_launches(1);
   return (int)cudaGetLastError();
 }
