@@ -59,7 +59,8 @@ size_t hq_skinny_part_elems(const hq_device_info* dev, int mY);
 int hq_panel_qrp(cudaStream_t stream, const hq_device_info* dev, int mp, int nc, int pivoting,
                  double* P, int ldp, double* tau, double* U, int ldu,
                  int* perm, double* part, size_t part_elems, double* rowbuf, unsigned* bar,
-                 int* err, unsigned spin_limit);
+                 int* err, unsigned spin_limit,
+                 int sqnorm);
 size_t hq_panel_part_elems(const hq_device_info* dev, int nc);
 
 /* ---- T factor of a forward columnwise block reflector (DLARFT) -----------

@@ -511,8 +511,10 @@ static int core_hqrrp_k(hq_ws* w, int m, int n, double* dA, int ldda, int* djpvt
     }
 
     /* Panel QR (pivoted within its b columns), U, tau. */
+    /* Mixed: squared column norms in the panel's pivoting (division-free
+     * LAWN 176 downdate); plain keeps LAPACK's formula. */
     CK(hq_panel_qrp(w->st, dev, mp, b, panel_piv, ABR, ldda, dtau + j, w->U, w->ldu, w->perm,
-                    w->part, w->part_elems, w->rowbuf, w->bar + 1, w->err, spin));
+                    w->part, w->part_elems, w->rowbuf, w->bar + 1, w->err, spin, w->mixed));
     if (w->mixed) CK(hq_set_diag(w->st, b, w->U, w->ldu, 0.0)); /* U' for the digit products */
     /* The panel's swaps on the rows above it and on the labels. */
     CK(hq_permute_cols(w->st, j, AR, ldda, b, w->perm, w->tmp, djpvt + j, w->label_tmp));
@@ -780,7 +782,7 @@ static int core_dgeqp4(hq_ws* w, int m, int n, double* dA, int ldda, int* hjp, i
     const int b = imin(FIXED_BLOCK, nf - j), mp = m - j;
     double* ABR = dA + j + (size_t)j * ldda;
     CK(hq_panel_qrp(w->st, dev, mp, b, 0, ABR, ldda, dtau + j, w->U, w->ldu, w->perm, w->part,
-                    w->part_elems, w->rowbuf, w->bar + 1, w->err, spin));
+                    w->part_elems, w->rowbuf, w->bar + 1, w->err, spin, 0));
     if (w->mixed) CK(hq_set_diag(w->st, b, w->U, w->ldu, 0.0)); /* U' for the digit products */
     int rc = block_reflector(w, mp, b, dtau + j, ABR + (size_t)b * ldda, ldda, n - j - b);
     if (rc) return rc;
@@ -806,7 +808,7 @@ static int core_dgeqp4(hq_ws* w, int m, int n, double* dA, int ldda, int* hjp, i
         return HQ_E_UNSUPPORTED;
       }
       CK(hq_panel_qrp(w->st, dev, mt, nt, 1, At, ldda, dtau + nf, NULL, w->ldu, w->perm,
-                      w->part, w->part_elems, w->rowbuf, w->bar + 1, w->err, spin));
+                      w->part, w->part_elems, w->rowbuf, w->bar + 1, w->err, spin, 0));
       CK(hq_permute_cols(w->st, nf, dA + (size_t)nf * ldda, ldda, nt, w->perm, w->tmp,
                          djp + nf, w->label_tmp));
     } else {

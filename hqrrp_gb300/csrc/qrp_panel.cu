@@ -54,6 +54,7 @@ struct PnArgs {
   int* err;
   unsigned spin_limit;
   int smem_mode, rloc_max, ldxs;
+  int sqnorm;  // keep squared norms (d^2 <- d^2 - r^2, LAWN 176's test without divisions)
 };
 
 // Candidate order for the pivot: larger norm, then lower column (idamax's
@@ -257,7 +258,7 @@ __global__ void __launch_bounds__(NT, 1) panel_qrp_kernel(PnArgs a) {
   if (!hq_grid_barrier(a.bar, a.err, epoch, a.spin_limit, &s_flag)) return;
   reduce_parts(epoch, nc);
   for (int k = tid; k < nc; k += NT) {
-    sd[k] = sqrt(sw[k]);
+    sd[k] = a.sqnorm ? sw[k] : sqrt(sw[k]);
     se[k] = sd[k];
   }
   __syncthreads();
@@ -357,16 +358,26 @@ __global__ void __launch_bounds__(NT, 1) panel_qrp_kernel(PnArgs a) {
       int flag = 0;
       double dk = sd[k];
       if (dk != 0.0) {
-        double t1 = fabs(r) / dk;
-        t1 = (1.0 + t1) * (1.0 - t1);
-        if (0.0 > t1) t1 = 0.0;
-        const double ratio = dk / se[k];
-        const double t2 = t1 * ratio * ratio;
-        if (t2 <= HQ_TOL3Z) {
-          flag = 1;
+        if (a.sqnorm) {
+          const double nd = fma(-r, r, dk);
+          if (nd <= HQ_TOL3Z * se[k]) {
+            flag = 1;
+          } else {
+            dk = nd;
+            sd[k] = dk;
+          }
         } else {
-          dk *= sqrt(t1);
-          sd[k] = dk;
+          double t1 = fabs(r) / dk;
+          t1 = (1.0 + t1) * (1.0 - t1);
+          if (0.0 > t1) t1 = 0.0;
+          const double ratio = dk / se[k];
+          const double t2 = t1 * ratio * ratio;
+          if (t2 <= HQ_TOL3Z) {
+            flag = 1;
+          } else {
+            dk *= sqrt(t1);
+            sd[k] = dk;
+          }
         }
       }
       sflag[k] = flag;
@@ -393,7 +404,7 @@ __global__ void __launch_bounds__(NT, 1) panel_qrp_kernel(PnArgs a) {
     reduce_parts(epoch, na);
     for (int k = s + 1 + tid; k < nc; k += NT) {
       if (sflag[k]) {
-        const double nv = (a.mp - s - 1 > 0) ? sqrt(sw[k - s]) : 0.0;
+        const double nv = (a.mp - s - 1 > 0) ? (a.sqnorm ? sw[k - s] : sqrt(sw[k - s])) : 0.0;
         sd[k] = nv;
         se[k] = nv;
         sflag[k] = 0;
@@ -478,7 +489,8 @@ extern "C" size_t hq_panel_part_elems(const hq_device_info* dev, int nc) {
 extern "C" int hq_panel_qrp(cudaStream_t stream, const hq_device_info* dev, int mp, int nc,
                             int pivoting, double* P, int ldp, double* tau,
                             double* U, int ldu, int* perm, double* part, size_t part_elems,
-                            double* rowbuf, unsigned* bar, int* err, unsigned spin_limit) {
+                            double* rowbuf, unsigned* bar, int* err, unsigned spin_limit,
+                            int sqnorm) {
   if (nc <= 0 || mp <= 0) return 0;
   if (nc > HQ_MAX_PANEL) return (int)cudaErrorInvalidValue;
   PnArgs a;
@@ -498,6 +510,7 @@ extern "C" int hq_panel_qrp(cudaStream_t stream, const hq_device_info* dev, int 
   a.bar = bar;
   a.err = err;
   a.spin_limit = spin_limit;
+  a.sqnorm = sqnorm;
   const int G = panel_grid(dev, mp);
   if ((size_t)2 * G * a.pstride + 2 * ((size_t)a.pstride + 8) > part_elems)
     return (int)cudaErrorInvalidValue;

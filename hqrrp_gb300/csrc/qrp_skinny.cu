@@ -283,7 +283,11 @@ __global__ void __launch_bounds__(NT, 1) skinny_qrp_kernel(SkArgs a) {
 // work): double for the plain path, float for the mixed path, whose sketch is
 // formed from two-digit BF16 operands (~16 significant bits) and only steers
 // pivots.  Norms, their LAWN 176 downdate and recomputation, and the
-// reflector scalars are FP64 in both.
+// reflector scalars are FP64 in both.  The mixed path keeps squared norms:
+// d^2 <- d^2 - r^2, recomputed when d^2 - r^2 <= tol3z e^2 -- LAPACK's test
+// t2 = (d^2 - r^2) / e^2 <= tol3z without its two divisions and square root
+// (~1.2k cycles of FP64 latency per stage on this GPU); the argmax of d^2 is
+// the argmax of d.
 __device__ __forceinline__ bool better_key(long long k1, int p1, long long k2, int p2) {
   return k1 > k2 || (k1 == k2 && p1 < p2);
 }
@@ -291,6 +295,7 @@ __device__ __forceinline__ bool better_key(long long k1, int p1, long long k2, i
 template <int RPT, typename T>
 __global__ void __launch_bounds__(NT, 1) skinny_qrp_reg_kernel(SkArgs a) {
   constexpr int NCH = RPT / 8;  // chunks of 8 registers = 16 rows
+  constexpr bool SQ = sizeof(T) == 4;  // mixed path: squared norms
   constexpr int NC = NT / 2;
   __shared__ __align__(16) double sv[2 * RPT];   // winner column (raw)
   __shared__ __align__(16) T sv2[2 * RPT];  // the reflector v
@@ -322,7 +327,7 @@ __global__ void __launch_bounds__(NT, 1) skinny_qrp_reg_kernel(SkArgs a) {
     }
     q += __shfl_xor_sync(0xffffffffu, q, 1);
     if (have && h == 0) {
-      sd[c] = sqrt(q);
+      sd[c] = SQ ? q : sqrt(q);
       se[c] = sd[c];
       spos[c] = c_lo + c;
     }
@@ -484,13 +489,20 @@ __global__ void __launch_bounds__(NT, 1) skinny_qrp_reg_kernel(SkArgs a) {
     if (tid < nloc && spos[tid] > s) {
       double dc = sd[tid];
       if (dc != 0.0) {
-        double t1 = fabs(srs[tid]) / dc;
-        t1 = (1.0 + t1) * (1.0 - t1);
-        if (0.0 > t1) t1 = 0.0;
-        const double ratio = dc / se[tid];
-        const double t2 = t1 * ratio * ratio;
-        if (t2 <= HQ_TOL3Z) flag = 1;
-        else sd[tid] = dc * sqrt(t1);
+        if (SQ) {
+          const double r = srs[tid];
+          const double nd = fma(-r, r, dc);
+          if (nd <= HQ_TOL3Z * se[tid]) flag = 1;
+          else sd[tid] = nd;
+        } else {
+          double t1 = fabs(srs[tid]) / dc;
+          t1 = (1.0 + t1) * (1.0 - t1);
+          if (0.0 > t1) t1 = 0.0;
+          const double ratio = dc / se[tid];
+          const double t2 = t1 * ratio * ratio;
+          if (t2 <= HQ_TOL3Z) flag = 1;
+          else sd[tid] = dc * sqrt(t1);
+        }
       }
     }
     if (tid < NC) sflag[tid] = flag;
@@ -503,7 +515,7 @@ __global__ void __launch_bounds__(NT, 1) skinny_qrp_reg_kernel(SkArgs a) {
           if (r > s) q2 = fma((double)x[i], (double)x[i], q2);
         }
         q2 += __shfl_xor_sync(pmask, q2, 1);
-        const double dc = (mY - s - 1 > 0) ? sqrt(q2) : 0.0;
+        const double dc = (mY - s - 1 > 0) ? (SQ ? q2 : sqrt(q2)) : 0.0;
         if (h == 0) {
           sd[c] = dc;
           se[c] = dc;
