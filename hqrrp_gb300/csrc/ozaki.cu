@@ -256,6 +256,95 @@ __global__ void __launch_bounds__(512) ozk_split_row_kernel(
   }
 }
 
+// Long rows (K > 16384): the row does not fit the registers of one CTA, so
+// the split takes two streaming passes -- the per-row scale exponent first,
+// then every 8-element chunk of every row independently (consecutive threads
+// take consecutive chunks of a row: coalesced 64-byte loads, 512-byte digit
+// stores per warp and slice).  Same output as the kernels above.
+__global__ void __launch_bounds__(256) ozk_rowmax_kernel(const double* __restrict__ X,
+                                                         long long rs, long long ks, int R, int K,
+                                                         int rows_total, int* __restrict__ exps) {
+  __shared__ long long s_max[8];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int r = blockIdx.x; r < rows_total; r += gridDim.x) {
+    long long mb = 0;
+    if (r < R) {
+      const double* xr = X + (long long)r * rs;
+      for (int k = tid; k < K; k += 256) {
+        const long long bb = __double_as_longlong(xr[(long long)k * ks]) & 0x7FFFFFFFFFFFFFFFLL;
+        mb = bb > mb ? bb : mb;
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const long long ob = __shfl_xor_sync(0xffffffffu, mb, o);
+      mb = ob > mb ? ob : mb;
+    }
+    if (lane == 0) s_max[warp] = mb;
+    __syncthreads();
+    if (tid == 0) {
+      for (int w = 1; w < 8; ++w) mb = s_max[w] > mb ? s_max[w] : mb;
+      mb = s_max[0] > mb ? s_max[0] : mb;
+      const int bexp = (int)(mb >> 52);
+      exps[r] = bexp == 0 ? 0 : bexp - 1022;
+    }
+    __syncthreads();
+  }
+}
+
+template <int S>
+__global__ void __launch_bounds__(256) ozk_split_chunk_kernel(
+    const double* __restrict__ X, long long rs, long long ks, int R, int K, int KB, int rows_total,
+    uint8_t* __restrict__ tiles, const int* __restrict__ exps) {
+  constexpr unsigned long long BIAS = 0x8080808080808080ULL >> (8 * (8 - S));
+  const int nchunk = KB * (TK / 8);
+  const long long kp = (long long)KB * TK;
+  const long long slice_bytes = (long long)rows_total * kp * 2;
+  const long long total = (long long)rows_total * nchunk;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(idx / nchunk), ch = (int)(idx % nchunk);
+    const int k0 = ch * 8;
+    const bool live = r < R;
+    const double* xr = X + (live ? (long long)r * rs : 0);
+    const int shift_base = 8 * S - 1076 - exps[r];
+    double v[8];
+    if (live && ks == 1 && k0 + 8 <= K && ((reinterpret_cast<uintptr_t>(xr + k0) & 15) == 0)) {
+      const double2* p2 = reinterpret_cast<const double2*>(xr + k0);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const double2 d = p2[j];
+        v[2 * j] = d.x;
+        v[2 * j + 1] = d.y;
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < 8; ++j) v[j] = (live && k0 + j < K) ? xr[(long long)(k0 + j) * ks] : 0.0;
+    }
+    unsigned long long W[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) W[j] = (unsigned long long)fixed_point(v[j], shift_base) + BIAS;
+    uint8_t* base = tiles + ((long long)r * kp + k0) * 2;
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+      const int p = S - 1 - s;
+      uint32_t w[4];
+#pragma unroll
+      for (int j = 0; j < 8; j += 2) {
+        uint32_t u0, u1;
+        if (p == S - 1) {
+          u0 = (uint32_t)(W[j] >> (8 * p));
+          u1 = (uint32_t)(W[j + 1] >> (8 * p));
+        } else {
+          u0 = (uint32_t)(W[j] >> (8 * p)) & 255u;
+          u1 = (uint32_t)(W[j + 1] >> (8 * p)) & 255u;
+        }
+        w[j >> 1] = __byte_perm(digit_scaled(u0, s), digit_scaled(u1, s), 0x7632);
+      }
+      *reinterpret_cast<uint4*>(base + (long long)s * slice_bytes) = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // GEMM
 
@@ -782,6 +871,17 @@ extern "C" int hq_ozk_split(cudaStream_t stream, const double* X, long long rs, 
   if (blocks > 4096) blocks = 4096;
   uint8_t* t = static_cast<uint8_t*>(tiles);
   constexpr int ROW_CPT = 4;
+  if (K > 512 * 8 * ROW_CPT && S == 7) {
+    int mblocks = rows_total < 8192 ? rows_total : 8192;
+    ozk_rowmax_kernel<<<mblocks, 256, 0, stream>>>(X, rs, ks, R, K, rows_total, exps);
+    const long long chunks = (long long)rows_total * KB * (TK / 8);
+    long long cblocks = (chunks + 255) / 256;
+    if (cblocks > 65536) cblocks = 65536;
+    ozk_split_chunk_kernel<7><<<(unsigned)cblocks, 256, 0, stream>>>(X, rs, ks, R, K, KB,
+                                                                      rows_total, t, exps);
+    hq_count_launches(2);
+    return (int)cudaGetLastError();
+  }
   if (K >= 4096 && K <= 512 * 8 * ROW_CPT && S == 7) {
     int rblocks = rows_total < 16384 ? rows_total : 16384;
     ozk_split_row_kernel<7, ROW_CPT><<<rblocks, 512, 0, stream>>>(X, rs, ks, R, K, TR, KB,

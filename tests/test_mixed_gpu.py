@@ -28,6 +28,7 @@ def _col(X):
     (128, 1000, 4000, "T", "N", 7),  # the W1 = U^T C shape (split K)
     (1000, 777, 128, "N", "T", 7),  # the C -= U W2 shape
     (513, 65, 2049, "N", "N", 7),
+    (128, 200, 20000, "T", "N", 7),  # rows longer than 16384: two-pass split
     (640, 640, 640, "N", "N", 4),
 ])
 def test_ozaki_dgemm_accuracy(hq, m, n, k, ta, tb, s):
