@@ -297,14 +297,14 @@ __global__ void __launch_bounds__(NT, 1) skinny_qrp_reg_kernel(SkArgs a) {
   constexpr int NCH = RPT / 8;  // chunks of 8 registers = 16 rows
   constexpr bool SQ = sizeof(T) == 4;  // mixed path: squared norms
   constexpr int NC = NT / 2;
-  __shared__ __align__(16) double sv[2 * RPT];   // winner column (raw)
+  __shared__ __align__(16) T sv[2 * RPT];   // winner column (raw; scaled in FP32)
   __shared__ __align__(16) T sv2[2 * RPT];  // the reflector v
   __shared__ long long s_bk[NWARP];
   __shared__ int s_bp[NWARP], s_bc[NWARP];
   __shared__ int spos[NC], sflag[NC];
   __shared__ double sd[NC], se[NC], srs[NC];
   __shared__ int s_flag, s_win_pos, s_win_cta, s_win_col;
-  __shared__ double s_tau, s_scale;
+  __shared__ T s_tau, s_scale;
   const int P = gridDim.x, cta = blockIdx.x, tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5, h = lane & 1;
   const unsigned pmask = 3u << (lane & 30);
@@ -316,16 +316,39 @@ __global__ void __launch_bounds__(NT, 1) skinny_qrp_reg_kernel(SkArgs a) {
   const bool have = c < nloc;
 
   T x[RPT];
+  // FP32 registers hold the column times 2^-ec (ec from its norm), so FP32's
+  // range never limits the input; unscale = 2^ec converts back (exact).
+  double unscale = 1.0;
   {
     const double* src = a.Y + (size_t)(c_lo + (have ? c : 0)) * a.ldy;
     double q = 0.0;
+    if constexpr (SQ) {
+#pragma unroll 8
+      for (int i = 0; i < RPT; ++i) {
+        const int r = 2 * i + h;
+        const double y = (have && r < mY) ? src[r] : 0.0;
+        q = fma(y, y, q);
+      }
+      q += __shfl_xor_sync(0xffffffffu, q, 1);
+      int eq = (int)((__double_as_longlong(q) >> 52) & 0x7FF) - 1023;  // q >= 0
+      if (eq < -1022) eq = -1022;
+      const int ec = eq / 2;
+      const double sc = __longlong_as_double((long long)(1023 - ec) << 52);
+      unscale = __longlong_as_double((long long)(1023 + ec) << 52);
 #pragma unroll
-    for (int i = 0; i < RPT; ++i) {
-      const int r = 2 * i + h;
-      x[i] = (have && r < mY) ? (T)src[r] : (T)0;
-      q = fma((double)x[i], (double)x[i], q);
+      for (int i = 0; i < RPT; ++i) {
+        const int r = 2 * i + h;
+        x[i] = (have && r < mY) ? (T)(src[r] * sc) : (T)0;
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < RPT; ++i) {
+        const int r = 2 * i + h;
+        x[i] = (have && r < mY) ? (T)src[r] : (T)0;
+        q = fma((double)x[i], (double)x[i], q);
+      }
+      q += __shfl_xor_sync(0xffffffffu, q, 1);
     }
-    q += __shfl_xor_sync(0xffffffffu, q, 1);
     if (have && h == 0) {
       sd[c] = SQ ? q : sqrt(q);
       se[c] = sd[c];
@@ -366,10 +389,11 @@ __global__ void __launch_bounds__(NT, 1) skinny_qrp_reg_kernel(SkArgs a) {
       hdr[2] = bc >= 0 ? c_lo + bc : -1;
     }
     if (bc >= 0 && c == bc) {
+      T* recd = reinterpret_cast<T*>(rec + HDR);
 #pragma unroll
       for (int i = 0; i < RPT; ++i) {
         const int r = 2 * i + h;
-        if (r >= s && r < mY) rec[HDR + r] = (double)x[i];
+        if (r >= s && r < mY) recd[r] = x[i];
       }
     }
   };
@@ -430,23 +454,39 @@ __global__ void __launch_bounds__(NT, 1) skinny_qrp_reg_kernel(SkArgs a) {
       if (cta == wcta && c_lo + tid == wcol) spos[tid] = s;
     }
     // Winner column, rows s..mY-1.
-    const double* wrec = recs + (size_t)wcta * a.rec + HDR;
-    for (int r = s + tid; r < mY; r += NT) sv[r] = hq_ldcg(wrec + r);
+    const T* wrec = reinterpret_cast<const T*>(recs + (size_t)wcta * a.rec + HDR);
+    for (int r = s + tid; r < mY; r += NT) sv[r] = __ldcg(wrec + r);
     __syncthreads();
     if (s + 1 == a.b) break;  // the pivots are complete; V is discarded
-    // Warp 0: tail norm, reflector (one lane), v = [1; scale * tail].
+    // Warp 0: tail norm, reflector (one lane), v = [1; scale * tail].  In
+    // FP32 the reflector of the scaled column is built directly (it does not
+    // depend on the column's scale): beta = -sign(alpha) sqrt(alpha^2 + q),
+    // tau = (beta - alpha) / beta, scale = 1 / (alpha - beta); tau = 0 when
+    // the tail is zero.
     if (warp == 0) {
-      double q = 0.0;
+      T q = (T)0;
       for (int r = s + 1 + lane; r < mY; r += 32) q = fma(sv[r], sv[r], q);
       q = hq_warp_sum(q);
       if (lane == 0) {
-        const HqReflector hr = hq_make_reflector_sq(sv[s], q);
-        s_tau = hr.tau;
-        s_scale = hr.scale;
+        if constexpr (SQ) {
+          const float alpha = sv[s];
+          float tau = 0.f, scale = 0.f;
+          if (q > 0.f) {
+            const float beta = -copysignf(sqrtf(fmaf(alpha, alpha, q)), alpha);
+            tau = (beta - alpha) / beta;
+            scale = 1.f / (alpha - beta);
+          }
+          s_tau = tau;
+          s_scale = scale;
+        } else {
+          const HqReflector hr = hq_make_reflector_sq(sv[s], q);
+          s_tau = hr.tau;
+          s_scale = hr.scale;
+        }
       }
       __syncwarp();
-      const double scale = s_scale;
-      for (int r = s + 1 + lane; r < mY; r += 32) sv2[r] = (T)(scale * sv[r]);
+      const T scale = s_scale;
+      for (int r = s + 1 + lane; r < mY; r += 32) sv2[r] = scale * sv[r];
       if (lane == 0) {
         sv2[s] = (T)1;
         if (s > 0) sv2[s - 1] = (T)0;
@@ -460,11 +500,26 @@ __global__ void __launch_bounds__(NT, 1) skinny_qrp_reg_kernel(SkArgs a) {
     if (active) {
       const int sch = s >> 4;  // first chunk holding a row >= s
       T w = (T)0;
+      if constexpr (SQ) {  // two chains: half the FP32 latency
+        T w1 = (T)0;
 #pragma unroll
-      for (int ch = 0; ch < NCH; ++ch) {
-        if (ch >= sch && 16 * ch < mY) {
+        for (int ch = 0; ch < NCH; ++ch) {
+          if (ch >= sch && 16 * ch < mY) {
 #pragma unroll
-          for (int j = 0; j < 8; ++j) w = fma(sv2[16 * ch + 2 * j + h], x[8 * ch + j], w);
+            for (int j = 0; j < 8; j += 2) {
+              w = fma(sv2[16 * ch + 2 * j + h], x[8 * ch + j], w);
+              w1 = fma(sv2[16 * ch + 2 * j + 2 + h], x[8 * ch + j + 1], w1);
+            }
+          }
+        }
+        w += w1;
+      } else {
+#pragma unroll
+        for (int ch = 0; ch < NCH; ++ch) {
+          if (ch >= sch && 16 * ch < mY) {
+#pragma unroll
+            for (int j = 0; j < 8; ++j) w = fma(sv2[16 * ch + 2 * j + h], x[8 * ch + j], w);
+          }
         }
       }
       w += __shfl_xor_sync(pmask, w, 1);
@@ -480,7 +535,7 @@ __global__ void __launch_bounds__(NT, 1) skinny_qrp_reg_kernel(SkArgs a) {
           }
         }
       }
-      if (h == (s & 1)) srs[c] = (double)xs_new;
+      if (h == (s & 1)) srs[c] = SQ ? (double)xs_new * unscale : (double)xs_new;
     }
     __syncthreads();
     // Norm downdate, one thread per column (LAWN 176); flagged norms are
@@ -509,12 +564,24 @@ __global__ void __launch_bounds__(NT, 1) skinny_qrp_reg_kernel(SkArgs a) {
     if (__syncthreads_or(flag)) {
       if (active && sflag[c]) {
         double q2 = 0.0;
+        if constexpr (SQ) {
+          float f0 = 0.f, f1 = 0.f;
 #pragma unroll
-        for (int i = 0; i < RPT; ++i) {
-          const int r = 2 * i + h;
-          if (r > s) q2 = fma((double)x[i], (double)x[i], q2);
+          for (int i = 0; i < RPT; i += 2) {
+            if (2 * i + h > s) f0 = fmaf(x[i], x[i], f0);
+            if (i + 1 < RPT && 2 * (i + 1) + h > s) f1 = fmaf(x[i + 1], x[i + 1], f1);
+          }
+          f0 += f1;
+          f0 += __shfl_xor_sync(pmask, f0, 1);
+          q2 = (double)f0 * (unscale * unscale);
+        } else {
+#pragma unroll
+          for (int i = 0; i < RPT; ++i) {
+            const int r = 2 * i + h;
+            if (r > s) q2 = fma((double)x[i], (double)x[i], q2);
+          }
+          q2 += __shfl_xor_sync(pmask, q2, 1);
         }
-        q2 += __shfl_xor_sync(pmask, q2, 1);
         const double dc = (mY - s - 1 > 0) ? (SQ ? q2 : sqrt(q2)) : 0.0;
         if (h == 0) {
           sd[c] = dc;
