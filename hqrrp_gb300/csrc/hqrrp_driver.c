@@ -175,6 +175,14 @@ typedef struct {
    * W1 = U^T C on st; created on first use, ordered by the two events. */
   cudaStream_t side;
   cudaEvent_t ev_gram, ev_t;
+  /* Host-pointer calls on pinned host memory: each block's final columns go
+   * back to the host on a copy stream while later blocks run (columns
+   * [j, j + b) are never touched again once block j's panel is done). */
+  double* drain_host;
+  const double* drain_dev;
+  int drain_lda, drain_ldda, drain_rows, drain_done;
+  cudaStream_t cp;
+  cudaEvent_t ev_cp;
 } hq_ws;
 
 /* Close the interval since the previous mark and charge it to `phase`. */
@@ -251,6 +259,15 @@ static void* ws_alloc(hq_ws* w, size_t bytes) {
 }
 
 static void ws_release(hq_ws* w) {
+  if (w->cp) {
+    /* The copy stream reads the matrix: it finishes before anything is freed. */
+    cudaEventRecord(w->ev_cp, w->cp);
+    cudaStreamWaitEvent(w->st, w->ev_cp, 0);
+    cudaStreamDestroy(w->cp);
+    cudaEventDestroy(w->ev_cp);
+    w->cp = NULL;
+    w->drain_host = NULL;
+  }
   if (w->side) {
     /* Nothing may be freed while the side stream could still use it. */
     cudaEventRecord(w->ev_t, w->side);
@@ -403,6 +420,58 @@ static int side_stream(hq_ws* w) {
   return HQ_OK;
 }
 
+/* Copy-back of finished columns for host-pointer calls.  drain_begin arms it
+ * when the host matrix is page-locked (an asynchronous copy from pageable
+ * memory would block the enqueueing thread); drain_cols sends columns
+ * [drain_done, c1) once the work on st that finishes them is enqueued;
+ * drain_finish sends the rest on st and orders st after the copy stream. */
+static void drain_begin(hq_ws* w, double* host, int lda, const double* dev, int ldda, int rows) {
+  struct cudaPointerAttributes at;
+  w->drain_host = NULL;
+  if (cudaPointerGetAttributes(&at, host) != cudaSuccess) {
+    cudaGetLastError(); /* pageable memory on older runtimes: not an error */
+    return;
+  }
+  if (at.type != cudaMemoryTypeHost) return;
+  w->drain_host = host;
+  w->drain_dev = dev;
+  w->drain_lda = lda;
+  w->drain_ldda = ldda;
+  w->drain_rows = rows;
+  w->drain_done = 0;
+}
+
+static int drain_cols(hq_ws* w, int c1) {
+  if (!w->drain_host || c1 <= w->drain_done) return HQ_OK;
+  if (!w->cp) {
+    CK(cudaStreamCreateWithFlags(&w->cp, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&w->ev_cp, cudaEventDisableTiming));
+  }
+  const int c0 = w->drain_done;
+  CK(cudaEventRecord(w->ev_cp, w->st));
+  CK(cudaStreamWaitEvent(w->cp, w->ev_cp, 0));
+  CK(cudaMemcpy2DAsync(w->drain_host + (size_t)c0 * w->drain_lda, sizeof(double) * w->drain_lda,
+                       w->drain_dev + (size_t)c0 * w->drain_ldda, sizeof(double) * w->drain_ldda,
+                       sizeof(double) * w->drain_rows, c1 - c0, cudaMemcpyDeviceToHost, w->cp));
+  w->drain_done = c1;
+  return HQ_OK;
+}
+
+/* The columns not yet sent (all of them when draining is off), on st. */
+static int drain_finish(hq_ws* w, double* host, int lda, const double* dev, int ldda, int rows,
+                        int n) {
+  const int c0 = w->drain_host ? w->drain_done : 0;
+  if (w->cp) {
+    CK(cudaEventRecord(w->ev_cp, w->cp));
+    CK(cudaStreamWaitEvent(w->st, w->ev_cp, 0));
+  }
+  if (c0 < n)
+    CK(cudaMemcpy2DAsync(host + (size_t)c0 * lda, sizeof(double) * lda, dev + (size_t)c0 * ldda,
+                         sizeof(double) * ldda, sizeof(double) * rows, n - c0,
+                         cudaMemcpyDeviceToHost, w->st));
+  return HQ_OK;
+}
+
 /* Build T for the b reflectors in U (mp rows) and apply Q^T from the left to
  * C (mp x nc2): the dlarfb('L','T','F','C') of ...var4.c:711-740.
  *
@@ -518,6 +587,11 @@ static int core_hqrrp_k(hq_ws* w, int m, int n, double* dA, int ldda, int* djpvt
     if (w->mixed) CK(hq_set_diag(w->st, b, w->U, w->ldu, 0.0)); /* U' for the digit products */
     /* The panel's swaps on the rows above it and on the labels. */
     CK(hq_permute_cols(w->st, j, AR, ldda, b, w->perm, w->tmp, djpvt + j, w->label_tmp));
+    /* Columns [j, j + b) are final: later blocks touch only columns >= j + b. */
+    if (w->drain_host) {
+      int rc = drain_cols(w, j + b);
+      if (rc) return rc;
+    }
     {
       double fl = 0.0;
       for (int s2 = 0; s2 < b; ++s2) fl += 4.0 * (mp - s2) * (b - s2 - 1);
@@ -620,10 +694,10 @@ static int hqrrp_host(int m, int n, double* A, int lda, int* jpvt, double* tau, 
   CKF(cudaMemcpyAsync(djp, jpvt, sizeof(int) * n, cudaMemcpyHostToDevice, st));
   if (G) CKF(cudaMemcpy2DAsync(dG, sizeof(double) * mY, G, sizeof(double) * ldg,
                                sizeof(double) * mY, m, cudaMemcpyHostToDevice, st));
+  if (!rc) drain_begin(&w, A, lda, dA, ldda, m);
   if (!rc) rc = core_hqrrp(&w, m, n, dA, ldda, djp, dtau, nb, pp, panel_piv, dG, mY, g_seed);
+  if (!rc) rc = drain_finish(&w, A, lda, dA, ldda, m, n);
   if (!rc) rc = ws_check(&w);
-  CKF(cudaMemcpy2DAsync(A, sizeof(double) * lda, dA, sizeof(double) * ldda, sizeof(double) * m, n,
-                        cudaMemcpyDeviceToHost, st));
   CKF(cudaMemcpyAsync(jpvt, djp, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
   CKF(cudaMemcpyAsync(tau, dtau, sizeof(double) * mn, cudaMemcpyDeviceToHost, st));
   ws_release(&w);
@@ -745,6 +819,9 @@ static int core_dgeqp4(hq_ws* w, int m, int n, double* dA, int ldda, int* hjp, i
     return HQ_E_NOMEM;
   }
   const int nfix = fixed_columns_front(n, hjp, src);
+  /* With fixed columns the rows above the free block are permuted at the
+   * end, so no column is final early: copy back in one piece. */
+  if (nfix > 0) w->drain_host = NULL;
   int np = 0;
   for (int k = 0; k < n; ++k)
     if (src[k] != k) {
@@ -889,10 +966,10 @@ HQ_API void dgeqp4(int* m, int* n, double* A, int* lda, int* jpvt, double* tau, 
   CKF(cudaMemcpy2DAsync(dA, sizeof(double) * ldda, A, sizeof(double) * LDA, sizeof(double) * M, N,
                         cudaMemcpyHostToDevice, st));
   int iws = 3 * N + 1;
+  if (!rc) drain_begin(&w, A, LDA, dA, ldda, M);
   if (!rc) rc = core_dgeqp4(&w, M, N, dA, ldda, hjp, djp, dtau, &iws);
+  if (!rc) rc = drain_finish(&w, A, LDA, dA, ldda, M, N);
   if (!rc) rc = ws_check(&w);
-  CKF(cudaMemcpy2DAsync(A, sizeof(double) * LDA, dA, sizeof(double) * ldda, sizeof(double) * M, N,
-                        cudaMemcpyDeviceToHost, st));
   CKF(cudaMemcpyAsync(jpvt, djp, sizeof(int) * N, cudaMemcpyDeviceToHost, st));
   CKF(cudaMemcpyAsync(tau, dtau, sizeof(double) * mn, cudaMemcpyDeviceToHost, st));
   ws_release(&w);

@@ -137,6 +137,54 @@ def test_hqrrp_lda_larger_than_m(hq, oracle_lib):
     assert_parity((buf[:m], jp, tau), want)
 
 
+@pytest.mark.parametrize("m,n,lda,nb,fixed", [
+    (1300, 1100, 1333, 64, None),   # tall, lda > m
+    (1000, 1300, 1000, 64, None),   # wide: the columns past min(m, n) go back at the end
+    (1024, 1024, 1024, 128, None),
+    (1100, 1050, 1100, 64, 9),      # dgeqp4 with fixed columns: one copy at the end
+])
+def test_pinned_host_buffers_match_pageable(hq, m, n, lda, nb, fixed):
+    """Page-locked host matrices are copied back column block by column block
+    while later blocks run; the result is bit-identical to the pageable-buffer
+    call (one copy at the end), for both reference entry points, and rows
+    m..lda-1 are left alone."""
+    import ctypes as C
+    import torch
+    dp, ip = C.POINTER(C.c_double), C.POINTER(C.c_int)
+    L = hq.load()
+    big = oracle.gaussian(lda, n, 31 + m)
+    ref = hq.hqrrp(big[:m], nb, 10, 1)
+    pin = torch.from_numpy(np.array(big.T)).pin_memory()   # (n, lda) = column-major lda x n
+    jp = np.arange(1, n + 1, dtype=np.int32)
+    tau = np.zeros(min(m, n))
+    rc = L.NoFLA_HQRRP_WY_blk_var4(m, n, C.cast(pin.data_ptr(), dp), lda, jp.ctypes.data_as(ip),
+                                   tau.ctypes.data_as(dp), nb, 10, 1)
+    assert rc == 0, hq.last_error()
+    got = pin.numpy().T
+    np.testing.assert_array_equal(got[:m], ref[0])
+    np.testing.assert_array_equal(got[m:], big[m:])
+    np.testing.assert_array_equal(jp, ref[1])
+    np.testing.assert_array_equal(tau, ref[2])
+
+    jin = None if fixed is None else np.array([i % fixed == 0 for i in range(n)], np.int32)
+    ref4 = hq.dgeqp4(big[:m], jin)
+    pin = torch.from_numpy(np.array(big.T)).pin_memory()
+    jp = np.zeros(n, np.int32) if jin is None else jin.copy()
+    tau = np.zeros(min(m, n))
+    lwork = max(3 * n + 1, 2 * n + (n + 1) * 32)
+    work = np.zeros(lwork)
+    mi, ni, li, lw, info = C.c_int(m), C.c_int(n), C.c_int(lda), C.c_int(lwork), C.c_int(0)
+    L.dgeqp4(C.byref(mi), C.byref(ni), C.cast(pin.data_ptr(), dp), C.byref(li),
+             jp.ctypes.data_as(ip), tau.ctypes.data_as(dp), work.ctypes.data_as(dp), C.byref(lw),
+             C.byref(info))
+    assert info.value == 0, hq.last_error()
+    got = pin.numpy().T
+    np.testing.assert_array_equal(got[:m], ref4[0])
+    np.testing.assert_array_equal(got[m:], big[m:])
+    np.testing.assert_array_equal(jp, ref4[1])
+    np.testing.assert_array_equal(tau, ref4[2])
+
+
 def test_device_pointer_entry(hq, oracle_lib):
     import torch
     m, n, nb, pp = 1000, 800, 64, 10
