@@ -62,6 +62,18 @@ int hq_panel_qrp(cudaStream_t stream, const hq_device_info* dev, int mp, int nc,
                  int* err, unsigned spin_limit,
                  int sqnorm);
 size_t hq_panel_part_elems(const hq_device_info* dev, int nc);
+/* Exchange area of the panel kernel for `ctas` CTAs and nc columns, in
+ * doubles: [2][ps][ctas] FP64 partials (initial and recomputed norms), then
+ * [3][ps][HQ_PANEL_FX_CS] 64-bit words of fixed-point stage sums (four used
+ * per column; the stride spreads the columns' atomics over cache lines,
+ * which measured 13 ms faster per 16384^2 factorization than packed words);
+ * ps = nc rounded up to even (plus 2). */
+#ifndef HQ_PANEL_FX_CS
+#define HQ_PANEL_FX_CS 16 /* one 128-byte line per column: fewer atomics per line */
+#endif
+#define HQ_PANEL_PART_ELEMS(ctas, nc) \
+  (2 * (size_t)(ctas) * (size_t)(((nc) + 2) & ~1) + \
+   3 * (size_t)HQ_PANEL_FX_CS * (size_t)(((nc) + 2) & ~1))
 
 /* ---- T factor of a forward columnwise block reflector (DLARFT) -----------
  * Z = U^T U (k x k, ldz) is given; writes T (k x k, ldt), zero below the
@@ -90,17 +102,23 @@ int hq_permute_cols(cudaStream_t stream, int rows, double* X, int ldx, int nc, c
 size_t hq_ozk_tile_bytes(int rows, int K, int S, int side);
 int hq_ozk_split(cudaStream_t stream, const double* X, long long rs, long long ks, int R, int K,
                  int S, int side, void* tiles, int* exps);
+/* The same split (S = 7) from each row's largest FP64 exponent field raw[r]
+ * (rows < R), computed elsewhere: one streaming pass. */
+int hq_ozk_split_raw(cudaStream_t stream, const double* X, long long rs, long long ks, int R,
+                     int K, int S, int side, void* tiles, int* exps, const int* raw);
 int hq_ozk_gemm(cudaStream_t stream, const hq_device_info* dev, int M, int N, int K, int S,
                 const void* Atiles, const int* ea, const void* Btiles, const int* eb, int mode,
                 double sign, double* C, long long crs, long long ccs, double* ws,
                 size_t ws_elems, int* err, unsigned spin_limit);
 /* K <= 256: persistent kernel with double-buffered TMEM; the N side must be
- * split with side 2 (32-row tiles). */
+ * split with side 2 (32-row tiles).  Mode 1 with colexp: colexp[c] (zeroed
+ * before) receives the largest exponent field of the new C(r, c) over rows
+ * r >= row_lo. */
 int hq_ozk_short_ok(int K);
 int hq_ozk_gemm_short(cudaStream_t stream, const hq_device_info* dev, int M, int N, int K, int S,
                       const void* Atiles, const int* ea, const void* Btiles, const int* eb,
-                      int mode, double sign, double* C, long long crs, long long ccs, int* err,
-                      unsigned spin_limit);
+                      int mode, double sign, double* C, long long crs, long long ccs,
+                      int* colexp, int row_lo, int* err, unsigned spin_limit);
 
 /* ---- Batched pivoted QR (one persistent launch, device work queue) -------
  * d_work: hq_qrp_batched_workspace(batch) bytes; ints [32..32+batch) hold the

@@ -154,7 +154,7 @@ static dev_state* current_device(void) {
 /* ------------------------------------------------------------------------ */
 /* Device workspace of one call.                                            */
 
-#define MAX_ALLOCS 32
+#define MAX_ALLOCS 64
 typedef struct {
   dev_state* ds;
   cudaStream_t st;
@@ -171,6 +171,16 @@ typedef struct {
   int mixed;      /* split-BF16 tensor-core block updates */
   void *ozA, *ozB; /* digit tiles of the two operands of a mixed product */
   int *ozea, *ozeb;
+  /* Mixed mode: per global column, the largest FP64 exponent field of the
+   * trailing matrix below the next block's diagonal, written by the epilogue
+   * of the update that produced it (and permuted with the columns), so the
+   * next block splits its trailing matrix in one streaming pass. */
+  int* colexp;
+  /* Mixed mode: U's digits, split once per block and shared by its products
+   * (U^T as the M side: Gram, W1 = U^T C, the sketch's B^T = U^T G_R^T; U as
+   * the M side: C -= U W2, G_R^T -= U B2^T). */
+  void *ozUT, *ozU;
+  int *ozUTe, *ozUe;
   /* Side stream (high priority) for the one-SM T factor, overlapped with
    * W1 = U^T C on st; created on first use, ordered by the two events. */
   cudaStream_t side;
@@ -345,10 +355,14 @@ static int ws_setup(hq_ws* w, int m, int n, int nb, int pp, int pw) {
   w->label_tmp = ws_alloc(w, sizeof(int) * (size_t)imax(n, 2 * kmax));
   w->err = ws_alloc(w, sizeof(int) * 2);
   w->bar = ws_alloc(w, sizeof(unsigned) * 2);
-  if (w->mixed && mY > 0) {
+  if (w->mixed) {
+    /* Digit buffers of the split products: the sketch's (mY > 0) and those of
+     * the block reflectors (HQRRP blocks and dgeqp4's fixed-column blocks). */
     const int S = OZK_SLICES, S2 = OZK_SKETCH_SLICES;
-    size_t a = hq_ozk_tile_bytes(n, m, S2, 0), b = ozk_b_bytes(mY, m, S2), t;
+    size_t a = mY > 0 ? hq_ozk_tile_bytes(n, m, S2, 0) : 0, b = mY > 0 ? ozk_b_bytes(mY, m, S2) : 0;
+    size_t t;
     if ((t = hq_ozk_tile_bytes(kmax, m, S, 0)) > a) a = t;
+    if ((t = hq_ozk_tile_bytes(kmax, kmax, S, 0)) > a) a = t; /* W2 = T^T W1 */
     if ((t = hq_ozk_tile_bytes(m, kmax, S, 0)) > a) a = t;
     if ((t = hq_ozk_tile_bytes(n, kmax, S, 0)) > a) a = t;
     if ((t = ozk_b_bytes(n, m, S)) > b) b = t;
@@ -363,6 +377,11 @@ static int ws_setup(hq_ws* w, int m, int n, int nb, int pp, int pw) {
     w->ozB = ws_alloc(w, b);
     w->ozea = ws_alloc(w, sizeof(int) * (size_t)rows);
     w->ozeb = ws_alloc(w, sizeof(int) * (size_t)rows);
+    w->colexp = ws_alloc(w, sizeof(int) * (size_t)(imax(n, 1) + 64));
+    w->ozUT = ws_alloc(w, hq_ozk_tile_bytes(kmax, m, S, 0));
+    w->ozU = ws_alloc(w, hq_ozk_tile_bytes(m, kmax, S, 0));
+    w->ozUTe = ws_alloc(w, sizeof(int) * (size_t)(kmax + 128));
+    w->ozUe = ws_alloc(w, sizeof(int) * (size_t)(imax(m, 1) + 128));
   }
   if (w->failed) return HQ_E_NOMEM;
   CK(cudaMemsetAsync(w->err, 0, sizeof(int) * 2, w->st));
@@ -390,23 +409,50 @@ static int ws_check(hq_ws* w) {
 
 /* sign * X Y^T (mode 0: written to C; mode 1: added to C) with split-BF16
  * tensor-core products: X has M rows (element (r, k) at X[r*xrs + k*xks]),
- * Y has N rows, both K long; C element (r, c) at C[r*crs + c*ccs]. */
+ * Y has N rows, both K long; C element (r, c) at C[r*crs + c*ccs].
+ * y_raw: Y's rows' largest exponent fields, when known (one-pass split);
+ * c_exp: short products in mode 1 write C's columns' largest exponent fields
+ * over rows >= c_row_lo there. */
+static int ozk_product_x(hq_ws* w, int S, int M, int N, int K, const double* X, long long xrs,
+                         long long xks, const double* Y, long long yrs, long long yks, int mode,
+                         double sign, double* Cm, long long crs, long long ccs, const int* y_raw,
+                         int* c_exp, int c_row_lo, const void* xt, const int* xe) {
+  if (M <= 0 || N <= 0) return HQ_OK;
+  const int short_k = hq_ozk_short_ok(K);
+  /* xt / xe: X already split (M side), e.g. U's digits shared by a block's
+   * products. */
+  const void* at = xt ? xt : w->ozA;
+  const int* ae = xt ? xe : w->ozea;
+  if (!xt) CK(hq_ozk_split(w->st, X, xrs, xks, M, K, S, 0, w->ozA, w->ozea));
+  if (y_raw)
+    CK(hq_ozk_split_raw(w->st, Y, yrs, yks, N, K, S, short_k ? 2 : 1, w->ozB, w->ozeb, y_raw));
+  else
+    CK(hq_ozk_split(w->st, Y, yrs, yks, N, K, S, short_k ? 2 : 1, w->ozB, w->ozeb));
+  prof_mark(w, PH_SPLIT, 0.0);
+  if (short_k)
+    CK(hq_ozk_gemm_short(w->st, &w->ds->dev, M, N, K, S, at, ae, w->ozB, w->ozeb, mode, sign, Cm,
+                         crs, ccs, c_exp, c_row_lo, w->err, spin_limit()));
+  else
+    CK(hq_ozk_gemm(w->st, &w->ds->dev, M, N, K, S, at, ae, w->ozB, w->ozeb, mode, sign, Cm, crs,
+                   ccs, w->ws, w->ws_elems, w->err, spin_limit()));
+  /* flops charged: the BF16 tensor work, S(S+1)/2 digit products */
+  prof_mark(w, PH_TENSOR, (double)S * (S + 1) * M * N * (double)K);
+  return HQ_OK;
+}
+
 static int ozk_product(hq_ws* w, int S, int M, int N, int K, const double* X, long long xrs,
                        long long xks, const double* Y, long long yrs, long long yks, int mode,
                        double sign, double* Cm, long long crs, long long ccs) {
-  if (M <= 0 || N <= 0) return HQ_OK;
-  const int short_k = hq_ozk_short_ok(K);
-  CK(hq_ozk_split(w->st, X, xrs, xks, M, K, S, 0, w->ozA, w->ozea));
-  CK(hq_ozk_split(w->st, Y, yrs, yks, N, K, S, short_k ? 2 : 1, w->ozB, w->ozeb));
+  return ozk_product_x(w, S, M, N, K, X, xrs, xks, Y, yrs, yks, mode, sign, Cm, crs, ccs, NULL,
+                       NULL, 0, NULL, NULL);
+}
+
+/* Split U' (mp x b, w->U) once for the block: as U'^T (b rows, K = mp) and
+ * as U' (mp rows, K = b), both M-side digit tiles. */
+static int split_block_u(hq_ws* w, int mp, int b) {
+  CK(hq_ozk_split(w->st, w->U, w->ldu, 1, b, mp, OZK_SLICES, 0, w->ozUT, w->ozUTe));
+  CK(hq_ozk_split(w->st, w->U, 1, w->ldu, mp, b, OZK_SLICES, 0, w->ozU, w->ozUe));
   prof_mark(w, PH_SPLIT, 0.0);
-  if (short_k)
-    CK(hq_ozk_gemm_short(w->st, &w->ds->dev, M, N, K, S, w->ozA, w->ozea, w->ozB, w->ozeb, mode,
-                         sign, Cm, crs, ccs, w->err, spin_limit()));
-  else
-    CK(hq_ozk_gemm(w->st, &w->ds->dev, M, N, K, S, w->ozA, w->ozea, w->ozB, w->ozeb, mode, sign,
-                   Cm, crs, ccs, w->ws, w->ws_elems, w->err, spin_limit()));
-  /* flops charged: the BF16 tensor work, S(S+1)/2 digit products */
-  prof_mark(w, PH_TENSOR, (double)S * (S + 1) * M * N * (double)K);
   return HQ_OK;
 }
 
@@ -482,11 +528,13 @@ static int drain_finish(hq_ws* w, double* host, int lda, const double* dev, int 
  * in FP64: U^T U = U'^T U' + L + L^T + I, U^T C = U'^T C + C[0:b, :],
  * U W2 = U' W2 + [W2; 0]. */
 static int block_reflector(hq_ws* w, int mp, int b, const double* tau, double* Cm, int ldc,
-                           int nc2) {
+                           int nc2, const int* cx_in, int* cx_out) {
   const hq_device_info* dev = &w->ds->dev;
   if (w->mixed) {
-    int rc = ozk_product(w, OZK_SLICES, b, b, mp, w->U, w->ldu, 1, w->U, w->ldu, 1, 0, 1.0, w->Z,
-                         1, w->ldz);
+    int rc = split_block_u(w, mp, b);
+    if (rc) return rc;
+    rc = ozk_product_x(w, OZK_SLICES, b, b, mp, w->U, w->ldu, 1, w->U, w->ldu, 1, 0, 1.0, w->Z, 1,
+                       w->ldz, NULL, NULL, 0, w->ozUT, w->ozUTe);
     if (rc) return rc;
     CK(hq_gram_unit_fix(w->st, b, w->U, w->ldu, w->Z, w->ldz));
   } else {
@@ -503,16 +551,19 @@ static int block_reflector(hq_ws* w, int mp, int b, const double* tau, double* C
   prof_mark(w, PH_PANEL, w->mixed ? 0.0 : 2.0 * mp * b * b);
   if (nc2 > 0 && w->mixed) {
     /* W1 = U^T C, W2 = T^T W1 and C -= U W2 on the tensor cores. */
-    int rc = ozk_product(w, OZK_SLICES, b, nc2, mp, w->U, w->ldu, 1, Cm, ldc, 1, 0, 1.0, w->W1,
-                         1, w->ldw);
+    /* cx_in: C's columns' largest exponent fields (from the previous update);
+     * cx_out: the same for the next block, over rows >= b of the new C. */
+    int rc = ozk_product_x(w, OZK_SLICES, b, nc2, mp, w->U, w->ldu, 1, Cm, ldc, 1, 0, 1.0,
+                           w->W1, 1, w->ldw, cx_in, NULL, 0, w->ozUT, w->ozUTe);
     if (rc) return rc;
     CK(hq_add_matrix(w->st, b, nc2, 1.0, Cm, ldc, w->W1, w->ldw));
     CK(cudaStreamWaitEvent(w->st, w->ev_t, 0));
     rc = ozk_product(w, OZK_SLICES, b, nc2, b, w->T, w->ldt, 1, w->W1, w->ldw, 1, 0, 1.0, w->W2, 1,
                      w->ldw);
     if (rc) return rc;
-    rc = ozk_product(w, OZK_SLICES, mp, nc2, b, w->U, 1, w->ldu, w->W2, w->ldw, 1, 1, -1.0, Cm, 1,
-                     ldc);
+    if (cx_out) CK(cudaMemsetAsync(cx_out, 0, sizeof(int) * (size_t)nc2, w->st));
+    rc = ozk_product_x(w, OZK_SLICES, mp, nc2, b, w->U, 1, w->ldu, w->W2, w->ldw, 1, 1, -1.0, Cm,
+                       1, ldc, NULL, cx_out, b, w->ozU, w->ozUe);
     if (rc) return rc;
     CK(hq_add_matrix(w->st, b, nc2, -1.0, w->W2, w->ldw, Cm, ldc));
   } else if (nc2 > 0) {
@@ -555,6 +606,7 @@ static int core_hqrrp_k(hq_ws* w, int m, int n, double* dA, int ldda, int* djpvt
     prof_mark(w, PH_SKETCH, 2.0 * mY * m * n);
   }
 
+  int cx_ok = 0; /* w->colexp holds the trailing columns' exponent fields */
   for (int j = 0; j < mn; j += nb) {
     const int b = imin(imin(nb, mn - j), imin(n - j, m - j));
     const int last = (j + nb >= m) || (j + nb >= n);
@@ -572,8 +624,8 @@ static int core_hqrrp_k(hq_ws* w, int m, int n, double* dA, int ldda, int* djpvt
                        w->part, w->part_elems, w->bar, w->err, spin, w->mixed));
       CK(hq_permute_pairs(w->st, m, AR, ldda, n - j, w->pairs, w->npairs, 2 * b, w->tmp,
                           djpvt + j, w->label_tmp));
-      CK(hq_permute_pairs(w->st, mY, YR, w->ldy, n - j, w->pairs, w->npairs, 2 * b, w->tmp, NULL,
-                          NULL));
+      CK(hq_permute_pairs(w->st, mY, YR, w->ldy, n - j, w->pairs, w->npairs, 2 * b, w->tmp,
+                          cx_ok ? w->colexp + j : NULL, cx_ok ? w->label_tmp : NULL));
       double fl = 0.0;
       for (int s2 = 0; s2 < b; ++s2) fl += 4.0 * (mY - s2) * (n - j - s2 - 1);
       prof_mark(w, PH_SELECT, fl);
@@ -599,8 +651,11 @@ static int core_hqrrp_k(hq_ws* w, int m, int n, double* dA, int ldda, int* djpvt
     }
 
     /* T and the trailing update [A12; A22] := Q^T [A12; A22]. */
-    int rc = block_reflector(w, mp, b, dtau + j, ABR + (size_t)b * ldda, ldda, nc2);
+    int* cx_out = (w->mixed && w->colexp && nc2 > 0) ? w->colexp + j + b : NULL;
+    int rc = block_reflector(w, mp, b, dtau + j, ABR + (size_t)b * ldda, ldda, nc2,
+                             cx_ok ? w->colexp + j + b : NULL, cx_out);
     if (rc) return rc;
+    cx_ok = cx_out != NULL;
 
     if (!last && !(final_block && mn < imin(m, n))) {
       /* Sketch downdate (...var4.c:617-708):
@@ -611,16 +666,16 @@ static int core_hqrrp_k(hq_ws* w, int m, int n, double* dA, int ldda, int* djpvt
          * long dimension is the 128-row tile side). */
         /* U holds U' (unit diagonal removed): Bm = G_R U' + G_R[:, 0:b] and
          * G_R -= B2 U'^T + [B2, 0]. */
-        int rc = ozk_product(w, OZK_SLICES, b, mY, mp, w->U, w->ldu, 1, GR, 1, w->ldg, 0, 1.0,
-                             w->Bm, w->ldb, 1);
+        int rc = ozk_product_x(w, OZK_SLICES, b, mY, mp, w->U, w->ldu, 1, GR, 1, w->ldg, 0, 1.0,
+                               w->Bm, w->ldb, 1, NULL, NULL, 0, w->ozUT, w->ozUTe);
         if (rc) return rc;
         CK(hq_add_matrix(w->st, mY, b, 1.0, GR, w->ldg, w->Bm, w->ldb));
         /* B2 = Bm T (mY x b x b): too few tiles for the FP64 kernel to fill the GPU. */
         rc = ozk_product(w, OZK_SLICES, mY, b, b, w->Bm, 1, w->ldb, w->T, w->ldt, 1, 0, 1.0, w->B2,
                          1, w->ldb);
         if (rc) return rc;
-        rc = ozk_product(w, OZK_SLICES, mp, mY, b, w->U, 1, w->ldu, w->B2, 1, w->ldb, 1, -1.0, GR,
-                         w->ldg, 1);
+        rc = ozk_product_x(w, OZK_SLICES, mp, mY, b, w->U, 1, w->ldu, w->B2, 1, w->ldb, 1, -1.0, GR,
+                           w->ldg, 1, NULL, NULL, 0, w->ozU, w->ozUe);
         if (rc) return rc;
         CK(hq_add_matrix(w->st, mY, b, -1.0, w->B2, w->ldb, GR, w->ldg));
         rc = ozk_product(w, OZK_SLICES, nc2, mY, b, ABR + (size_t)b * ldda, ldda, 1, GR, 1, w->ldg,
@@ -861,7 +916,8 @@ static int core_dgeqp4(hq_ws* w, int m, int n, double* dA, int ldda, int* hjp, i
     CK(hq_panel_qrp(w->st, dev, mp, b, 0, ABR, ldda, dtau + j, w->U, w->ldu, w->perm, w->part,
                     w->part_elems, w->rowbuf, w->bar + 1, w->err, spin, 0));
     if (w->mixed) CK(hq_set_diag(w->st, b, w->U, w->ldu, 0.0)); /* U' for the digit products */
-    int rc = block_reflector(w, mp, b, dtau + j, ABR + (size_t)b * ldda, ldda, n - j - b);
+    int rc = block_reflector(w, mp, b, dtau + j, ABR + (size_t)b * ldda, ldda, n - j - b, NULL,
+                             NULL);
     if (rc) return rc;
   }
   if (nf > 0) {

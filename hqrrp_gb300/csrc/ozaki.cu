@@ -294,7 +294,7 @@ __global__ void __launch_bounds__(256) ozk_rowmax_kernel(const double* __restric
 template <int S>
 __global__ void __launch_bounds__(256) ozk_split_chunk_kernel(
     const double* __restrict__ X, long long rs, long long ks, int R, int K, int KB, int rows_total,
-    uint8_t* __restrict__ tiles, const int* __restrict__ exps) {
+    uint8_t* __restrict__ tiles, int* __restrict__ exps, const int* __restrict__ raw) {
   constexpr unsigned long long BIAS = 0x8080808080808080ULL >> (8 * (8 - S));
   const int nchunk = KB * (TK / 8);
   const long long kp = (long long)KB * TK;
@@ -306,7 +306,15 @@ __global__ void __launch_bounds__(256) ozk_split_chunk_kernel(
     const int k0 = ch * 8;
     const bool live = r < R;
     const double* xr = X + (live ? (long long)r * rs : 0);
-    const int shift_base = 8 * S - 1076 - exps[r];
+    int e;
+    if (raw != nullptr) {  // the rows' largest exponent fields, known in advance
+      const int bexp = live ? raw[r] : 0;
+      e = bexp == 0 ? 0 : bexp - 1022;
+      if (ch == 0) exps[r] = e;
+    } else {
+      e = exps[r];
+    }
+    const int shift_base = 8 * S - 1076 - e;
     double v[8];
     if (live && ks == 1 && k0 + 8 <= K && ((reinterpret_cast<uintptr_t>(xr + k0) & 15) == 0)) {
       const double2* p2 = reinterpret_cast<const double2*>(xr + k0);
@@ -363,6 +371,10 @@ struct OzkArgs {
   int stages;  // 2 or 3, whatever fits in shared memory
   int* err;
   unsigned spin_limit;
+  // Short kernel, mode 1: when set, colexp[c] gets the largest exponent field
+  // of the new C over rows >= row_lo of column c (atomicMax; zeroed before).
+  int* colexp;
+  int row_lo;
 };
 
 __device__ __forceinline__ void mbar_init(uint64_t* b, unsigned count) {
@@ -491,10 +503,11 @@ __device__ __forceinline__ void drain_tmem(uint32_t tacc, int nacc, float* hi, f
 // first prefetched into L2 (no registers held), then read in batches of 8
 // with every load of a batch issued before its stores.
 __device__ __forceinline__ void write_row(const OzkArgs& a, int r, int n0, double* crow,
-                                          const float* hi, const float* lo) {
+                                          const float* hi, const float* lo, bool live) {
   const unsigned neg = a.sign < 0.0 ? 1u : 0u;
-  const int er = a.ea[r] - 14;
-  if (a.mode == 1) {
+  const int er = live ? a.ea[r] - 14 : 0;
+  const bool counted = live && r >= a.row_lo;
+  if (a.mode == 1 && live) {
 #pragma unroll
     for (int j = 0; j < EPI_COLS; ++j)
       if (n0 + j < a.N)
@@ -507,17 +520,29 @@ __device__ __forceinline__ void write_row(const OzkArgs& a, int r, int n0, doubl
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       const int n = n0 + c8 + j;
-      ek[j] = n < a.N ? er + a.eb[n] : 0;
-      cv[j] = (a.mode == 1 && n < a.N) ? crow[(long long)n * a.ccs] : 0.0;
+      ek[j] = (live && n < a.N) ? er + a.eb[n] : 0;
+      cv[j] = (a.mode == 1 && live && n < a.N) ? crow[(long long)n * a.ccs] : 0.0;
     }
+    unsigned fx[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       const int n = n0 + c8 + j;
-      if (n < a.N) {
+      fx[j] = 0u;
+      if (live && n < a.N) {
         // sign * (hi + lo) * 2^ek: the two exact conversions take no FP64
         // instruction, their sum one (exact: hi + lo fits in FP64).
         const double v = f32_scaled(hi[c8 + j], ek[j], neg) + f32_scaled(lo[c8 + j], ek[j], neg);
-        crow[(long long)n * a.ccs] = a.mode == 0 ? v : cv[j] + v;
+        const double out = a.mode == 0 ? v : cv[j] + v;
+        crow[(long long)n * a.ccs] = out;
+        if (counted) fx[j] = (unsigned)((__double_as_longlong(out) >> 52) & 0x7FF);
+      }
+    }
+    if (a.colexp != nullptr) {  // kernel-uniform; every lane of the warp is here
+      const int lane = threadIdx.x & 31;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const unsigned m = __reduce_max_sync(0xffffffffu, fx[j]);
+        if (lane == j && m != 0u) atomicMax(a.colexp + n0 + c8 + j, (int)m);
       }
     }
   }
@@ -662,7 +687,7 @@ __global__ void __launch_bounds__(NT, 1) ozk_gemm_kernel(OzkArgs a,
       const int r = mt * TM + (warp & 3) * 32 + lane;
       if (r < a.M)
         write_row(a, r, nt * TN + col0, a.C + (long long)r * a.crs + (long long)z * a.zstride, hi,
-                  lo);
+                  lo, true);
     }
   }
 
@@ -797,7 +822,9 @@ __global__ void __launch_bounds__(NT, 1) ozk_gemm_short_kernel(
     const uint32_t tacc = tbase + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)col0;
     int lt = 0;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++lt) {
-      if (!mbar_wait(&tfull, lt & 1, lim, &s_abort)) {
+      // One outcome per warp: the TMEM loads and the exponent reduction
+      // below are warp-wide, so no lane may leave the loop alone.
+      if (!__all_sync(0xffffffffu, mbar_wait(&tfull, lt & 1, lim, &s_abort))) {
         s_abort = 1;
         break;
       }
@@ -814,7 +841,10 @@ __global__ void __launch_bounds__(NT, 1) ozk_gemm_short_kernel(
       mbar_arrive(&tempty);
       const int mt = t / NTL, nt = t % NTL;
       const int r = mt * TM + (warp & 3) * 32 + lane;
-      if (r < a.M) write_row(a, r, nt * TN + col0, a.C + (long long)r * a.crs, hi, lo);
+      // Every lane takes part (the column-exponent reduction is warp-wide);
+      // rows past M only skip their loads and stores.
+      write_row(a, r, nt * TN + col0, a.C + (long long)(r < a.M ? r : 0) * a.crs, hi, lo,
+                r < a.M);
     }
   }
 
@@ -878,7 +908,7 @@ extern "C" int hq_ozk_split(cudaStream_t stream, const double* X, long long rs, 
     long long cblocks = (chunks + 255) / 256;
     if (cblocks > 65536) cblocks = 65536;
     ozk_split_chunk_kernel<7><<<(unsigned)cblocks, 256, 0, stream>>>(X, rs, ks, R, K, KB,
-                                                                      rows_total, t, exps);
+                                                                      rows_total, t, exps, nullptr);
     hq_count_launches(2);
     return (int)cudaGetLastError();
   }
@@ -899,6 +929,27 @@ extern "C" int hq_ozk_split(cudaStream_t stream, const double* X, long long rs, 
     HQ_SPLIT_CASE(6) HQ_SPLIT_CASE(7)
 #undef HQ_SPLIT_CASE
   }
+  hq_count_launches(1);
+  return (int)cudaGetLastError();
+}
+
+// The split with each row's largest exponent field already known (raw[r],
+// e.g. produced by the epilogue of the update that wrote X): one streaming
+// pass, no row maximum.  exps receives the scale exponents as hq_ozk_split
+// writes them.
+extern "C" int hq_ozk_split_raw(cudaStream_t stream, const double* X, long long rs, long long ks,
+                                int R, int K, int S, int side, void* tiles, int* exps,
+                                const int* raw) {
+  if (R <= 0 || K <= 0) return 0;
+  if (S != 7) return (int)cudaErrorInvalidValue;
+  const int TR = side == 0 ? TM : (side == 2 ? TN_SHORT : TN);
+  const int RT = (R + TR - 1) / TR, KB = (K + TK - 1) / TK;
+  const int rows_total = RT * TR;
+  const long long chunks = (long long)rows_total * KB * (TK / 8);
+  long long cblocks = (chunks + 255) / 256;
+  if (cblocks > 65536) cblocks = 65536;
+  ozk_split_chunk_kernel<7><<<(unsigned)cblocks, 256, 0, stream>>>(
+      X, rs, ks, R, K, KB, rows_total, static_cast<uint8_t*>(tiles), exps, raw);
   hq_count_launches(1);
   return (int)cudaGetLastError();
 }
@@ -964,6 +1015,8 @@ extern "C" int hq_ozk_gemm(cudaStream_t stream, const hq_device_info* dev, int M
   a.sign = sign;
   a.err = err;
   a.spin_limit = spin_limit;
+  a.colexp = nullptr;
+  a.row_lo = 0;
   if (Z > 1) {
     a.C = ws;
     a.crs = 1;
@@ -1009,8 +1062,8 @@ extern "C" int hq_ozk_short_ok(int K) { return K > 0 && K <= KB_PER_DRAIN * TK; 
 extern "C" int hq_ozk_gemm_short(cudaStream_t stream, const hq_device_info* dev, int M, int N,
                                  int K, int S, const void* Atiles, const int* ea,
                                  const void* Btiles, const int* eb, int mode, double sign,
-                                 double* C, long long crs, long long ccs, int* err,
-                                 unsigned spin_limit) {
+                                 double* C, long long crs, long long ccs, int* colexp, int row_lo,
+                                 int* err, unsigned spin_limit) {
   if (M <= 0 || N <= 0 || K <= 0) return 0;
   if (S < 1 || S > 7 || !hq_ozk_short_ok(K)) return (int)cudaErrorInvalidValue;
   constexpr int TNV = TN_SHORT;
@@ -1032,6 +1085,8 @@ extern "C" int hq_ozk_gemm_short(cudaStream_t stream, const hq_device_info* dev,
   a.crs = crs;
   a.ccs = ccs;
   a.zstride = 0;
+  a.colexp = mode == 1 ? colexp : nullptr;
+  a.row_lo = row_lo;
   const size_t per_stage = (size_t)S * (A_TILE + B_TILE);
   int stages = MAX_STAGES;
   while (stages > 2 && (size_t)stages * per_stage + 1024 > dev->smem_optin) --stages;

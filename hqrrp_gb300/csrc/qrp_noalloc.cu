@@ -26,8 +26,7 @@
 
 namespace {
 
-constexpr size_t kPartElems =
-    2ull * NOALLOC_MAX_CTAS * ((NOALLOC_MAX_N + 2) & ~1) + 2ull * (((NOALLOC_MAX_N + 2) & ~1) + 8);
+constexpr size_t kPartElems = HQ_PANEL_PART_ELEMS(NOALLOC_MAX_CTAS, NOALLOC_MAX_N);
 constexpr size_t kRowbufElems = 2ull * NOALLOC_MAX_N;
 constexpr size_t kPermElems = NOALLOC_MAX_N / 2;  // NOALLOC_MAX_N ints
 constexpr size_t kFlagElems = 2;                  // barrier counter, error word
@@ -38,7 +37,7 @@ constexpr int kRcCuda = 1, kRcDevice = 2, kRcUnsupported = 3;
 
 }  // namespace
 
-// 2 x 160 x 258 + 2 x 266 + 512 + 128 + 2 doubles = 669,872 bytes (654 KiB)
+// 2 x 160 x 258 + 48 x 258 + 512 + 128 + 2 doubles = 764,688 bytes (747 KiB)
 // per GPU.
 static __device__ __align__(256) double hq_noalloc_scratch[kScratchElems];
 

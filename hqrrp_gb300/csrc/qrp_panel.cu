@@ -18,16 +18,22 @@
 // exchange: every CTA publishes, for its slab, the dot products of the pivot
 // column with all not-yet-factored columns (the first of which is the pivot
 // column's squared norm); the owner of the pivot row also publishes that row.
-// FP64 issue is the scarce resource on this GPU, so the sums are not formed
-// redundantly in every CTA: after a barrier, CTA c sums column c's partials
-// (laid out contiguously, one coalesced load per lane), the CTA of column 0
-// also builds the reflector, and after a second barrier every CTA loads the
-// sums, the reflector and the pivot row together.  The sums are taken in a
-// fixed order, so results are reproducible.  The slab is then updated without
-// further communication.  The norm downdate of the trailing columns carries
-// the warp-level argmax of the next pivot.
-// The rare norm recomputation costs one more barrier in the stages that need
-// it.
+// The partials are summed as fixed-point integers: each CTA adds its partial
+// of column k, exactly, as three 48-bit limbs of a 144-bit integer in units
+// of 2^ue_k (ue_k from the two columns' norms, which bound every partial and
+// their sum by Cauchy-Schwarz) to three 64-bit words with L2 atomics.
+// Integer addition is associative, so the order of the atomics does not
+// matter: the sums are the same in every run, and exact up to the truncation
+// below 2^ue_k (2^-133 of the bound, far below FP64 rounding of the
+// partials).  One grid barrier per stage then suffices: every CTA reads the
+// words of all columns, converts them to FP64 and builds the reflector
+// itself (identical inputs, identical results), with no reduce-scatter and
+// no second barrier -- FP64 adds of 152 partials per column in every CTA
+// would cost microseconds on this GPU's FP64 pipe, integer atomics do not.
+// The slab is then updated without further communication.  The norm
+// downdate of the trailing columns carries the warp-level argmax of the next
+// pivot.  The rare norm recomputation costs one more barrier in the stages
+// that need it (FP64 partials, summed in a fixed order in every CTA).
 #include "hq_common.cuh"
 
 namespace {
@@ -46,8 +52,8 @@ struct PnArgs {
   double* U;
   int ldu;
   int* perm;
-  double* part;  // [2][pstride][grid] partials (column q's contiguous), then
-                 // [2][pstride + 8] reduced sums with tau, scale, beta after them
+  double* part;  // [2][pstride][grid] partials (column q's contiguous)
+  unsigned long long* acc;  // [3][pstride][FX_CS] fixed-point stage sums
   int pstride;
   double* rowbuf;  // [2][nc]
   unsigned* bar;
@@ -56,6 +62,90 @@ struct PnArgs {
   int smem_mode, rloc_max, ldxs;
   int sqnorm;  // keep squared norms (d^2 <- d^2 - r^2, LAWN 176's test without divisions)
 };
+
+// Fixed-point stage sums: words 0..2 of a column are limbs (bits 48i..48i+47
+// of the integer, as signed 64-bit accumulators: 16 bits of headroom take
+// the carries of up to 160 CTAs), word 3 counts non-finite partials.
+constexpr int FX_W = 4;
+constexpr int FX_CS = HQ_PANEL_FX_CS;  // words between consecutive columns
+#ifndef HQ_PANEL_FX_WS
+#define HQ_PANEL_FX_WS 1
+#endif
+constexpr int FX_WS = HQ_PANEL_FX_WS;  // words between a column's words
+constexpr int FX_MARGIN = 8;  // bound slack (2^8) over the Cauchy-Schwarz bound
+constexpr unsigned long long FX_MASK = (1ull << 48) - 1;
+
+// e(x) with 0 <= x < 2^e(x) for finite x >= 0 (zero and subnormals: 2^-1022).
+__device__ __forceinline__ int fx_exp(double x) {
+  const int b = (int)((__double_as_longlong(x) >> 52) & 0x7FF);
+  return b == 0 ? -1022 : b - 1022;
+}
+
+// Unit exponent of the stage sum of columns p (pivot) and k: the bound on
+// |sum| is sqrt(ep * ek) (squared norms) or ep * ek (norms), and the integer
+// of the sum stays below 2^(141 - FX_MARGIN).
+__device__ __forceinline__ int fx_unit(double ep, double ek, int sqnorm) {
+  const int e = sqnorm ? (fx_exp(ep) + fx_exp(ek) + 1) >> 1 : fx_exp(ep) + fx_exp(ek);
+  return e + FX_MARGIN - 141;
+}
+
+// Adds t / 2^ue, truncated to an integer, to the words w (L2 atomics).
+__device__ __forceinline__ void fx_add(unsigned long long* w, double t, int ue) {
+  const long long bits = __double_as_longlong(t);
+  const int ex = (int)((bits >> 52) & 0x7FF);
+  if (ex == 0x7FF) {
+    atomicAdd(w + 3 * FX_WS, 1ull);
+    return;
+  }
+  if (ex == 0) return;  // zero (subnormal partials lie below the units in use)
+  const unsigned long long mant = (unsigned long long)(bits & 0xFFFFFFFFFFFFFLL) | (1ull << 52);
+  const int sh = ex - 1075 - ue;  // t = mant * 2^(ex - 1075) = mant * 2^sh units
+  unsigned long long M;
+  int s0;
+  if (sh >= 0) {
+    M = mant;
+    s0 = sh;
+  } else if (sh > -53) {
+    M = mant >> (-sh);
+    s0 = 0;
+  } else {
+    return;
+  }
+  if (s0 > 91) {  // beyond the bound: only from non-finite norms
+    atomicAdd(w + 3 * FX_WS, 1ull);
+    return;
+  }
+  const int L = s0 / 48, off = s0 - 48 * L;  // M * 2^off spans limbs L..L+2
+  unsigned long long p0 = (M << off) & FX_MASK;
+  unsigned long long p1 = (M >> (48 - off)) & FX_MASK;
+  unsigned long long p2 = (96 - off) < 64 ? (M >> (96 - off)) : 0ull;
+  if (bits < 0) {
+    p0 = 0ull - p0;
+    p1 = 0ull - p1;
+    p2 = 0ull - p2;
+  }
+  if (p0) atomicAdd(w + L * FX_WS, p0);
+  if (p1 && L + 1 < 3) atomicAdd(w + (L + 1) * FX_WS, p1);
+  if (p2 && L + 2 < 3) atomicAdd(w + (L + 2) * FX_WS, p2);
+}
+
+// The sum in the words w (carries normalised in integers, then two FMAs).
+// All four words are loaded before any is used (one L2 round trip).
+__device__ __forceinline__ double fx_value(const unsigned long long* w, int ue) {
+  const unsigned long long nf = __ldcg(w + 3 * FX_WS);
+  long long l0 = (long long)__ldcg(w), l1 = (long long)__ldcg(w + FX_WS);
+  long long l2 = (long long)__ldcg(w + 2 * FX_WS);
+  if (nf != 0ull) return __longlong_as_double(0x7FF8000000000000LL);
+  long long c = l0 >> 48;  // arithmetic shift: floor
+  l0 -= c * (1LL << 48);
+  l1 += c;
+  c = l1 >> 48;
+  l1 -= c * (1LL << 48);
+  l2 += c;
+  const double two48 = 281474976710656.0;
+  const double hi = fma((double)l2, two48, (double)l1);
+  return scalbn(fma(hi, two48, (double)l0), ue);
+}
 
 // Candidate order for the pivot: larger norm, then lower column (idamax's
 // first maximum); NaN never wins.
@@ -101,28 +191,34 @@ __global__ void __launch_bounds__(NT, 1) panel_qrp_kernel(PnArgs a) {
   }
   // A valid permutation is in place before any wait: if a barrier gives up
   // and the kernel returns early, the gathers that follow still read indices
-  // within range.
-  if (cta == 0)
+  // within range.  Stage sums of stage s go to words buffer s % 3; buffers 0
+  // and 1 start at zero (ordered before stage 0 by the first barrier), and
+  // CTA 0 clears buffer (s + 1) % 3 during stage s: its last readers passed
+  // the barrier of stage s - 1, its first writers come after that of stage s.
+  if (cta == 0) {
     for (int k = tid; k < nc; k += NT) a.perm[k] = k;
+    for (int i = tid; i < 2 * a.pstride * FX_CS; i += NT) a.acc[i] = 0ull;
+  }
   __syncthreads();
 
   unsigned epoch = 0;
   auto part_w = [&](unsigned e) { return a.part + (size_t)(e & 1) * a.pstride * G + cta; };
   auto part_r = [&](unsigned e) { return a.part + (size_t)(e & 1) * a.pstride * G; };
   // The pivot row of stage s goes to buffer s & 1: it is read after the
-  // stage's second barrier, and the next write to the same buffer (stage
-  // s + 2) comes after a barrier every reader has passed.
+  // stage's barrier, and the next write to the same buffer (stage s + 2)
+  // comes after a barrier every reader has passed.
   auto rowbuf = [&](int s) { return a.rowbuf + (size_t)(s & 1) * nc; };
-  auto red_buf = [&](unsigned e) {
-    return a.part + (size_t)2 * a.pstride * G + (size_t)(e & 1) * (a.pstride + 8);
-  };
+  auto fx_buf = [&](int s) { return a.acc + (size_t)(s % 3) * a.pstride * FX_CS; };
 
   // Slab-local sums over rows with global index > lo_row of x_i * X[i, k]
   // (x = column xs, or column k itself when xs < 0) for k in [k0, nc),
   // skipping columns without sflag when use_mask; column k's sum goes to
-  // out[(k - k0) * G].  Below NT columns, `groups` adjacent lanes share a
-  // column and combine by shuffles.
-  auto slab_dots = [&](int xs, int k0, int lo_row, bool use_mask, double* out) {
+  // out[(k - k0) * G], or, when fx is given, is added to the fixed-point
+  // words fx[(k - k0) * FX_CS..] in the units of columns xs and k (xs's norm
+  // bound in sep).  Below NT columns, `groups` adjacent lanes share a column
+  // and combine by shuffles.
+  auto slab_dots = [&](int xs, int k0, int lo_row, bool use_mask, double* out,
+                       unsigned long long* fx, double sep) {
     const int na = nc - k0;
     const int i0 = max(0, lo_row + 1 - r_lo);
     int groups = 1;
@@ -150,7 +246,10 @@ __global__ void __launch_bounds__(NT, 1) panel_qrp_kernel(PnArgs a) {
         t += t1;
       }
       for (int o = groups >> 1; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-      if (g == 0 && q < na) out[(size_t)q * G] = t;
+      if (g == 0 && q < na) {
+        if (fx) fx_add(fx + (size_t)q * FX_CS, t, fx_unit(sep, se[k], a.sqnorm));
+        else out[(size_t)q * G] = t;
+      }
     }
   };
 
@@ -184,50 +283,23 @@ __global__ void __launch_bounds__(NT, 1) panel_qrp_kernel(PnArgs a) {
     __syncthreads();
   };
 
-  // Reduce-scatter of stage s: warp w of CTA c sums columns c + (w + i*NWARP)*G
-  // (same fixed order as above) into the published sums; column 0's reducer
-  // also builds the reflector from the tail norm and the pivot-row entry.
-  auto reduce_scatter = [&](unsigned e, int na, int s) {
-    for (int q = cta + warp * G; q < na; q += NWARP * G) {
-      const double* col = part_r(e) + (size_t)q * G;
-      double v[CB];
-#pragma unroll
-      for (int j = 0; j < CB; ++j) {
-        const int c = lane + 32 * j;
-        v[j] = c < G ? hq_ldcg(col + c) : 0.0;
-      }
-      const double alpha = (q == 0 && lane == 0) ? hq_ldcg(rowbuf(s) + s) : 0.0;
-      double t = v[0];
-#pragma unroll
-      for (int j = 1; j < CB; ++j) t += v[j];
-      t = hq_warp_sum(t);
-      if (lane == 0) {
-        double* red = red_buf(e);
-        red[q] = t;
-        if (q == 0) {
-          const HqReflector h = hq_make_reflector_sq(alpha, (a.mp - s > 1) ? t : 0.0);
-          red[a.pstride] = h.tau;
-          red[a.pstride + 1] = h.scale;
-          red[a.pstride + 2] = h.beta;
-        }
-      }
-    }
-  };
-
-  // All-gather after the second barrier: sums, pivot row, reflector.
-  auto gather_sums = [&](unsigned e, int na, int s) {
-    const double* red = red_buf(e);
+  // After the stage's barrier: the sums of all columns from the fixed-point
+  // words, the pivot row, and the reflector (built by thread 0 of every CTA
+  // from the same inputs).
+  auto gather_sums = [&](int na, int s, double sep) {
+    const unsigned long long* fx = fx_buf(s);
     const double* rb = rowbuf(s) + s;
     for (int q = tid; q < na; q += NT) {
-      const double t = hq_ldcg(red + q);
+      const double t = fx_value(fx + (size_t)q * FX_CS, fx_unit(sep, se[s + q], a.sqnorm));
       const double r = hq_ldcg(rb + q);
       sw[q] = t;
       srow[q] = r;
-    }
-    if (tid == 0) {
-      s_tau = hq_ldcg(red + a.pstride);
-      s_scale = hq_ldcg(red + a.pstride + 1);
-      s_beta = hq_ldcg(red + a.pstride + 2);
+      if (q == 0) {
+        const HqReflector h = hq_make_reflector_sq(r, (a.mp - s > 1) ? t : 0.0);
+        s_tau = h.tau;
+        s_scale = h.scale;
+        s_beta = h.beta;
+      }
     }
     __syncthreads();
   };
@@ -253,7 +325,7 @@ __global__ void __launch_bounds__(NT, 1) panel_qrp_kernel(PnArgs a) {
   };
 
   // Initial norms over the whole panel.
-  slab_dots(-1, 0, -1, false, part_w(epoch + 1));
+  slab_dots(-1, 0, -1, false, part_w(epoch + 1), nullptr, 0.0);
   ++epoch;
   if (!hq_grid_barrier(a.bar, a.err, epoch, a.spin_limit, &s_flag)) return;
   reduce_parts(epoch, nc);
@@ -266,7 +338,9 @@ __global__ void __launch_bounds__(NT, 1) panel_qrp_kernel(PnArgs a) {
 
   for (int s = 0; s < a.ns; ++s) {
     const int na = nc - s;
-    // 1. Swap the pivot column into place (columns, labels, copied norms).
+    // 1. Swap the pivot column into place (columns, labels, copied norms;
+    //    se[s] takes the pivot's own value, which bounds its stage sums --
+    //    position s's norms are not read again otherwise).
     if (kp != s) {
       double* c1 = X + (size_t)s * ldx;
       double* c2 = X + (size_t)kp * ldx;
@@ -279,15 +353,23 @@ __global__ void __launch_bounds__(NT, 1) panel_qrp_kernel(PnArgs a) {
         const int t = sperm[s];
         sperm[s] = sperm[kp];
         sperm[kp] = t;
+        const double pse = se[kp];
         sd[kp] = sd[s];
         se[kp] = se[s];
+        se[s] = pse;
       }
       __syncthreads();
     }
+    const double sep = se[s];
 
-    // 2. Publish slab dots with the pivot column (rows > s) and, from the
-    //    owner of row s, that row.
-    slab_dots(s, s, s, false, part_w(epoch + 1));
+    // 2. Add the slab dots with the pivot column (rows > s) to the stage's
+    //    fixed-point sums; the owner of row s publishes that row.  CTA 0
+    //    clears the words of stage s + 1.
+    if (cta == 0) {
+      unsigned long long* nx = fx_buf(s + 1);
+      for (int i = tid; i < na * FX_CS; i += NT) nx[i] = 0ull;
+    }
+    slab_dots(s, s, s, false, nullptr, fx_buf(s), sep);
     if (s >= r_lo && s < r_hi) {
       double* rb = rowbuf(s);
       for (int k = s + tid; k < nc; k += NT) rb[k] = X[(s - r_lo) + (size_t)k * ldx];
@@ -295,13 +377,8 @@ __global__ void __launch_bounds__(NT, 1) panel_qrp_kernel(PnArgs a) {
     ++epoch;
     if (!hq_grid_barrier(a.bar, a.err, epoch, a.spin_limit, &s_flag)) return;
 
-    // 3. Reduce-scatter, second barrier, all-gather of the sums and of the
-    //    reflector (built once, by column 0's reducer).
-    const unsigned e_pub = epoch;
-    reduce_scatter(e_pub, na, s);
-    ++epoch;
-    if (!hq_grid_barrier(a.bar, a.err, epoch, a.spin_limit, &s_flag)) return;
-    gather_sums(e_pub, na, s);
+    // 3. Sums, pivot row and reflector in every CTA.
+    gather_sums(na, s, sep);
     const double tau = s_tau, scale = s_scale;
     if (cta == 0 && tid == 0) a.tau[s] = tau;
     {
@@ -398,7 +475,7 @@ __global__ void __launch_bounds__(NT, 1) panel_qrp_kernel(PnArgs a) {
       kp = (bk == 0x7fffffff || bd < 0) ? s + 1 : bk;
       continue;  // s_bd is next written after the next stage's grid barrier
     }
-    slab_dots(-1, s, s, true, part_w(epoch + 1));
+    slab_dots(-1, s, s, true, part_w(epoch + 1), nullptr, 0.0);
     ++epoch;
     if (!hq_grid_barrier(a.bar, a.err, epoch, a.spin_limit, &s_flag)) return;
     reduce_parts(epoch, na);
@@ -482,8 +559,7 @@ __global__ void larft_kernel(int k, const double* __restrict__ Z, int ldz,
 }  // namespace
 
 extern "C" size_t hq_panel_part_elems(const hq_device_info* dev, int nc) {
-  const size_t ps = (size_t)((nc + 2) & ~1);
-  return (size_t)2 * dev->num_sms * ps + 2 * (ps + 8);
+  return HQ_PANEL_PART_ELEMS(dev->num_sms, nc);
 }
 
 extern "C" int hq_panel_qrp(cudaStream_t stream, const hq_device_info* dev, int mp, int nc,
@@ -512,8 +588,8 @@ extern "C" int hq_panel_qrp(cudaStream_t stream, const hq_device_info* dev, int 
   a.spin_limit = spin_limit;
   a.sqnorm = sqnorm;
   const int G = panel_grid(dev, mp);
-  if ((size_t)2 * G * a.pstride + 2 * ((size_t)a.pstride + 8) > part_elems)
-    return (int)cudaErrorInvalidValue;
+  if (HQ_PANEL_PART_ELEMS(G, nc) > part_elems) return (int)cudaErrorInvalidValue;
+  a.acc = reinterpret_cast<unsigned long long*>(part + (size_t)2 * G * a.pstride);
   a.rloc_max = (mp + G - 1) / G;
   a.ldxs = a.rloc_max | 1;
   const size_t fixed = sizeof(double) * (4 * (size_t)nc) + sizeof(int) * (2 * (size_t)nc + 2);

@@ -96,7 +96,7 @@ int hqrrp_gb300_dgeqp4_device(int m, int n, double* dA, int ldda, int* d_jpvt, d
  * that cannot allocate at this point: a process that has given all device
  * memory to its own arena, or a loop that cannot afford the device
  * synchronisation of cudaMalloc/cudaFree or their failure under memory
- * pressure.  Its scratch is a fixed 654 KiB __device__ array held by every GPU
+ * pressure.  Its scratch is a fixed 747 KiB __device__ array held by every GPU
  * that loads the library until exit, shared by all calls: calls that overlap
  * on the GPU race and must be serialised by the caller.  The first call on a
  * device does a one-time set-up (scratch address lookup) and should come

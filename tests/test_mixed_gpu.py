@@ -104,3 +104,18 @@ def test_mixed_dgeqp4_fixed_columns(mixed):
     assert sorted(jpvt[:21]) == [i + 1 for i in range(0, 1050, 50)]
     res, orth, _ = oracle.quality(A, Af, jpvt, tau)
     assert res <= 1e-13 and orth <= 1e-12
+
+
+@pytest.mark.parametrize("m,n,every", [(400, 300, 7), (300, 520, 9), (120, 90, 4)])
+def test_mixed_dgeqp4_small_path_fixed_columns(mixed, m, n, every):
+    """Below dgeqp4's dgeqp3 threshold, with fixed columns: the fixed block's
+    trailing update runs as split-BF16 products, the rest as the pivoted
+    FP64 panel kernel."""
+    A = oracle.gaussian(m, n, m + 3 * n)
+    jp = np.array([1 if i % every == 0 else 0 for i in range(n)], np.int32)
+    nf = int(jp.sum())
+    Af, jpvt, tau, info, _ = mixed.dgeqp4(A, jp)
+    assert info == 0
+    assert sorted(jpvt[:nf]) == [i + 1 for i in range(0, n, every)]
+    res, orth, _ = oracle.quality(A, Af, jpvt, tau)
+    assert res <= 1e-13 and orth <= 1e-12, (res, orth)
