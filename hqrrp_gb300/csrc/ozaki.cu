@@ -566,6 +566,43 @@ __device__ __forceinline__ void issue_block(uint32_t tb, uint64_t da0, uint64_t 
   }
 }
 
+// The same for seven digits, fully unrolled: every descriptor offset, TMEM
+// column and accumulate flag is a constant, so the single issuing thread
+// spends its time on tcgen05.mma instead of loop and index arithmetic.
+// FIRST: the first K block after a drain (the first MMA into each
+// accumulator overwrites it; with seven digits every accumulator's first
+// pair has s = 0).
+template <bool FIRST>
+__device__ __forceinline__ void issue_block7(uint32_t tb, uint64_t da0, uint64_t db0,
+                                             uint32_t idesc) {
+  constexpr int S = 7;
+#pragma unroll
+  for (int s = 0; s < S; ++s) {
+#pragma unroll
+    for (int t = 0; t < S - s; ++t) {
+      const int L = s + t;
+      const int q = L < MAX_ACC - 1 ? L : MAX_ACC - 1;
+#pragma unroll
+      for (int kk = 0; kk < TK / 16; ++kk) {
+        const bool overwrite = FIRST && s == 0 && kk == 0 && t <= MAX_ACC - 1;
+        mma_bf16(tb + (uint32_t)(q * TN), da0 + (uint64_t)((s * A_TILE) >> 4) + 2 * kk,
+                 db0 + (uint64_t)((t * B_TILE) >> 4) + 2 * kk, idesc, overwrite ? 0u : 1u);
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ void issue_any(uint32_t tb, uint64_t da0, uint64_t db0, int S,
+                                          uint32_t idesc, unsigned& fresh) {
+  if (S == 7) {
+    if (fresh == 0xFFu) issue_block7<true>(tb, da0, db0, idesc);
+    else issue_block7<false>(tb, da0, db0, idesc);
+    fresh = 0u;
+  } else {
+    issue_block(tb, da0, db0, S, idesc, fresh);
+  }
+}
+
 __global__ void __launch_bounds__(NT, 1) ozk_gemm_kernel(OzkArgs a,
                                                         const __grid_constant__ CUtensorMap tmA,
                                                         const __grid_constant__ CUtensorMap tmB) {
@@ -642,8 +679,8 @@ __global__ void __launch_bounds__(NT, 1) ozk_gemm_kernel(OzkArgs a,
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        issue_block(tbase, sw64_desc(smem_u32(sA + st * a_stage)),
-                    sw64_desc(smem_u32(sB + st * b_stage)), S, idesc, fresh);
+        issue_any(tbase, sw64_desc(smem_u32(sA + st * a_stage)),
+                  sw64_desc(smem_u32(sB + st * b_stage)), S, idesc, fresh);
         mma_issued = 1;
         mma_commit(&empty_bar[st]);
         if ((i + 1) % KB_PER_DRAIN == 0 && i + 1 < nkb) {
@@ -804,8 +841,8 @@ __global__ void __launch_bounds__(NT, 1) ozk_gemm_short_kernel(
             break;
           }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-          issue_block(tbase, sw64_desc(smem_u32(sA + st * a_stage)),
-                      sw64_desc(smem_u32(sB + st * b_stage)), S, idesc, fresh);
+          issue_any(tbase, sw64_desc(smem_u32(sA + st * a_stage)),
+                    sw64_desc(smem_u32(sB + st * b_stage)), S, idesc, fresh);
           mma_issued = 1;
           mma_commit(&empty_bar[st]);
         }
