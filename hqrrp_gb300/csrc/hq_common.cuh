@@ -11,9 +11,6 @@
 #include "hq_internal.h"
 
 #define HQ_WARP 32
-#ifndef HQ_BARRIER_SLEEP_NS
-#define HQ_BARRIER_SLEEP_NS 32 /* back-off between polls of a grid barrier */
-#endif
 
 __device__ __forceinline__ unsigned hq_ld_acquire(const unsigned* p) {
   unsigned v;
@@ -67,9 +64,7 @@ __device__ __forceinline__ bool hq_grid_barrier(unsigned* counter, int* err, uns
         ok = 0;
         break;
       }
-#if HQ_BARRIER_SLEEP_NS > 0
-      __nanosleep(HQ_BARRIER_SLEEP_NS);
-#endif
+      __nanosleep(32);
     }
     *s_flag = ok;
   }

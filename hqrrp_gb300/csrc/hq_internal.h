@@ -68,9 +68,7 @@ size_t hq_panel_part_elems(const hq_device_info* dev, int nc);
  * per column; the stride spreads the columns' atomics over cache lines,
  * which measured 13 ms faster per 16384^2 factorization than packed words);
  * ps = nc rounded up to even (plus 2). */
-#ifndef HQ_PANEL_FX_CS
 #define HQ_PANEL_FX_CS 16 /* one 128-byte line per column: fewer atomics per line */
-#endif
 #define HQ_PANEL_PART_ELEMS(ctas, nc) \
   (2 * (size_t)(ctas) * (size_t)(((nc) + 2) & ~1) + \
    3 * (size_t)HQ_PANEL_FX_CS * (size_t)(((nc) + 2) & ~1))

@@ -68,10 +68,6 @@ struct PnArgs {
 // the carries of up to 160 CTAs), word 3 counts non-finite partials.
 constexpr int FX_W = 4;
 constexpr int FX_CS = HQ_PANEL_FX_CS;  // words between consecutive columns
-#ifndef HQ_PANEL_FX_WS
-#define HQ_PANEL_FX_WS 1
-#endif
-constexpr int FX_WS = HQ_PANEL_FX_WS;  // words between a column's words
 constexpr int FX_MARGIN = 8;  // bound slack (2^8) over the Cauchy-Schwarz bound
 constexpr unsigned long long FX_MASK = (1ull << 48) - 1;
 
@@ -94,7 +90,7 @@ __device__ __forceinline__ void fx_add(unsigned long long* w, double t, int ue) 
   const long long bits = __double_as_longlong(t);
   const int ex = (int)((bits >> 52) & 0x7FF);
   if (ex == 0x7FF) {
-    atomicAdd(w + 3 * FX_WS, 1ull);
+    atomicAdd(w + 3, 1ull);
     return;
   }
   if (ex == 0) return;  // zero (subnormal partials lie below the units in use)
@@ -112,7 +108,7 @@ __device__ __forceinline__ void fx_add(unsigned long long* w, double t, int ue) 
     return;
   }
   if (s0 > 91) {  // beyond the bound: only from non-finite norms
-    atomicAdd(w + 3 * FX_WS, 1ull);
+    atomicAdd(w + 3, 1ull);
     return;
   }
   const int L = s0 / 48, off = s0 - 48 * L;  // M * 2^off spans limbs L..L+2
@@ -124,17 +120,17 @@ __device__ __forceinline__ void fx_add(unsigned long long* w, double t, int ue) 
     p1 = 0ull - p1;
     p2 = 0ull - p2;
   }
-  if (p0) atomicAdd(w + L * FX_WS, p0);
-  if (p1 && L + 1 < 3) atomicAdd(w + (L + 1) * FX_WS, p1);
-  if (p2 && L + 2 < 3) atomicAdd(w + (L + 2) * FX_WS, p2);
+  if (p0) atomicAdd(w + L, p0);
+  if (p1 && L + 1 < 3) atomicAdd(w + L + 1, p1);
+  if (p2 && L + 2 < 3) atomicAdd(w + L + 2, p2);
 }
 
 // The sum in the words w (carries normalised in integers, then two FMAs).
 // All four words are loaded before any is used (one L2 round trip).
 __device__ __forceinline__ double fx_value(const unsigned long long* w, int ue) {
-  const unsigned long long nf = __ldcg(w + 3 * FX_WS);
-  long long l0 = (long long)__ldcg(w), l1 = (long long)__ldcg(w + FX_WS);
-  long long l2 = (long long)__ldcg(w + 2 * FX_WS);
+  const unsigned long long nf = __ldcg(w + 3);
+  long long l0 = (long long)__ldcg(w), l1 = (long long)__ldcg(w + 1);
+  long long l2 = (long long)__ldcg(w + 2);
   if (nf != 0ull) return __longlong_as_double(0x7FF8000000000000LL);
   long long c = l0 >> 48;  // arithmetic shift: floor
   l0 -= c * (1LL << 48);
