@@ -10,9 +10,13 @@
  *
  * All matrices are column-major FP64.  The host-pointer entry points copy A to
  * the GPU, factor it there and copy A, jpvt and tau back; every arithmetic
- * step runs in this library's CUDA kernels (no CPU LAPACK).  When the CUDA
- * device or a kernel fails they report it (info / return code, message from
- * hqrrp_gb300_last_error()) instead of falling back to the CPU.
+ * step runs in this library's CUDA kernels (no CPU LAPACK).  When A is in
+ * page-locked host memory (cudaHostAlloc / cudaHostRegister), each block's
+ * finished columns are copied back while later blocks are factored, so the
+ * copy costs little beyond the factorization; pageable A is copied back once
+ * at the end.  When the CUDA device or a kernel fails they report it (info /
+ * return code, message from hqrrp_gb300_last_error()) instead of falling back
+ * to the CPU; a page-locked A may then hold partial results.
  */
 #ifndef HQRRP_GB300_H
 #define HQRRP_GB300_H
@@ -54,12 +58,15 @@ int NoFLA_HQRRP_WY_blk_var4(int m_A, int n_A, double* buff_A, int ldim_A, int* b
 /* ---- Extensions (no reference counterpart unless stated) ----------------- */
 
 /* Precision of the block updates: 0 = plain FP64 (default), 1 = mixed: the
- * sketch Y = G A from two-digit BF16 operands, and the trailing update
- * (dlarfb) and the sketch downdate as split-BF16 products on the tensor cores
- * (seven digits per operand, exact FP32 accumulation per level, recombined in
- * FP64); the panel, its reflectors and tau, the norm downdating, T and W2 =
- * T^T W1 stay FP64.  HQRRP_GB300_PRECISION=mixed in the environment selects 1
- * at first use.  Returns the previous value, or -1 for an unknown mode. */
+ * sketch Y = G A from two-digit BF16 operands; the trailing update (dlarfb:
+ * U^T C, T^T W1, C -= U W2), the Gram matrix U^T U and the sketch downdate as
+ * split-BF16 products on the tensor cores (seven digits per operand, exact
+ * FP32 accumulation per level, recombined in FP64); pivot selection on the
+ * sketch applies its reflectors in FP32 to a power-of-two-scaled copy of each
+ * column.  The panel, its reflectors and tau, all column norms and their
+ * downdating, and T stay FP64.  HQRRP_GB300_PRECISION=mixed in the
+ * environment selects 1 at first use.  Returns the previous value, or -1 for
+ * an unknown mode. */
 int hqrrp_gb300_set_precision(int mode);
 
 /* Seed of the device Philox sketch used when no sketch is supplied. */
