@@ -35,6 +35,7 @@
 // pivot.  The rare norm recomputation costs one more barrier in the stages
 // that need it (FP64 partials, summed in a fixed order in every CTA).
 #include "hq_common.cuh"
+#include "hq_fixedpoint.h"
 
 namespace {
 
@@ -63,84 +64,36 @@ struct PnArgs {
   int sqnorm;  // keep squared norms (d^2 <- d^2 - r^2, LAWN 176's test without divisions)
 };
 
-// Fixed-point stage sums: words 0..2 of a column are limbs (bits 48i..48i+47
-// of the integer, as signed 64-bit accumulators: 16 bits of headroom take
-// the carries of up to 160 CTAs), word 3 counts non-finite partials.
-constexpr int FX_W = 4;
+// Fixed-point stage sums (hq_fixedpoint.h): words 0..2 of a column are the
+// limbs' signed 64-bit accumulators, word 3 counts non-finite partials.
 constexpr int FX_CS = HQ_PANEL_FX_CS;  // words between consecutive columns
-constexpr int FX_MARGIN = 8;  // bound slack (2^8) over the Cauchy-Schwarz bound
-constexpr unsigned long long FX_MASK = (1ull << 48) - 1;
 
-// e(x) with 0 <= x < 2^e(x) for finite x >= 0 (zero and subnormals: 2^-1022).
-__device__ __forceinline__ int fx_exp(double x) {
-  const int b = (int)((__double_as_longlong(x) >> 52) & 0x7FF);
-  return b == 0 ? -1022 : b - 1022;
-}
-
-// Unit exponent of the stage sum of columns p (pivot) and k: the bound on
-// |sum| is sqrt(ep * ek) (squared norms) or ep * ek (norms), and the integer
-// of the sum stays below 2^(141 - FX_MARGIN).
 __device__ __forceinline__ int fx_unit(double ep, double ek, int sqnorm) {
-  const int e = sqnorm ? (fx_exp(ep) + fx_exp(ek) + 1) >> 1 : fx_exp(ep) + fx_exp(ek);
-  return e + FX_MARGIN - 141;
+  return hq_fx_unit(ep, ek, sqnorm);
 }
 
 // Adds t / 2^ue, truncated to an integer, to the words w (L2 atomics).
 __device__ __forceinline__ void fx_add(unsigned long long* w, double t, int ue) {
-  const long long bits = __double_as_longlong(t);
-  const int ex = (int)((bits >> 52) & 0x7FF);
-  if (ex == 0x7FF) {
+  unsigned long long p[3];
+  int L = 0;
+  const int rc = hq_fx_split(t, ue, p, &L);
+  if (rc == 2) {
     atomicAdd(w + 3, 1ull);
-    return;
+  } else if (rc == 1) {
+    if (p[0]) atomicAdd(w + L, p[0]);
+    if (p[1] && L + 1 < 3) atomicAdd(w + L + 1, p[1]);
+    if (p[2] && L + 2 < 3) atomicAdd(w + L + 2, p[2]);
   }
-  if (ex == 0) return;  // zero (subnormal partials lie below the units in use)
-  const unsigned long long mant = (unsigned long long)(bits & 0xFFFFFFFFFFFFFLL) | (1ull << 52);
-  const int sh = ex - 1075 - ue;  // t = mant * 2^(ex - 1075) = mant * 2^sh units
-  unsigned long long M;
-  int s0;
-  if (sh >= 0) {
-    M = mant;
-    s0 = sh;
-  } else if (sh > -53) {
-    M = mant >> (-sh);
-    s0 = 0;
-  } else {
-    return;
-  }
-  if (s0 > 91) {  // beyond the bound: only from non-finite norms
-    atomicAdd(w + 3, 1ull);
-    return;
-  }
-  const int L = s0 / 48, off = s0 - 48 * L;  // M * 2^off spans limbs L..L+2
-  unsigned long long p0 = (M << off) & FX_MASK;
-  unsigned long long p1 = (M >> (48 - off)) & FX_MASK;
-  unsigned long long p2 = (96 - off) < 64 ? (M >> (96 - off)) : 0ull;
-  if (bits < 0) {
-    p0 = 0ull - p0;
-    p1 = 0ull - p1;
-    p2 = 0ull - p2;
-  }
-  if (p0) atomicAdd(w + L, p0);
-  if (p1 && L + 1 < 3) atomicAdd(w + L + 1, p1);
-  if (p2 && L + 2 < 3) atomicAdd(w + L + 2, p2);
 }
 
-// The sum in the words w (carries normalised in integers, then two FMAs).
-// All four words are loaded before any is used (one L2 round trip).
+// The sum in the words w; all four words are loaded before any is used (one
+// L2 round trip).
 __device__ __forceinline__ double fx_value(const unsigned long long* w, int ue) {
   const unsigned long long nf = __ldcg(w + 3);
-  long long l0 = (long long)__ldcg(w), l1 = (long long)__ldcg(w + 1);
-  long long l2 = (long long)__ldcg(w + 2);
+  const long long l0 = (long long)__ldcg(w), l1 = (long long)__ldcg(w + 1);
+  const long long l2 = (long long)__ldcg(w + 2);
   if (nf != 0ull) return __longlong_as_double(0x7FF8000000000000LL);
-  long long c = l0 >> 48;  // arithmetic shift: floor
-  l0 -= c * (1LL << 48);
-  l1 += c;
-  c = l1 >> 48;
-  l1 -= c * (1LL << 48);
-  l2 += c;
-  const double two48 = 281474976710656.0;
-  const double hi = fma((double)l2, two48, (double)l1);
-  return scalbn(fma(hi, two48, (double)l0), ue);
+  return hq_fx_combine(l0, l1, l2, ue);
 }
 
 // Candidate order for the pivot: larger norm, then lower column (idamax's
