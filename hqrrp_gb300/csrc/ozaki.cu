@@ -31,10 +31,11 @@
 // pattern the MMA descriptors name (rows of 64 B, 8-row atoms of 512 B).
 // M tile 128 rows, N tile 80, K block 32.
 //
-// The GEMM kernel is warp-specialised: warp 4 issues the bulk copies into a
-// 3-stage (2 for seven digits) ring, one thread of warp 5 issues tcgen05.mma (cta_group::1,
-// kind::f16, 128 x 64 x 16) into TMEM, warps 0-3 drain TMEM (tcgen05.ld,
-// 32 lanes each) and write the output.  Every wait is bounded; on expiry the
+// The GEMM kernels are warp-specialised: warp 20 issues the bulk copies into a
+// 3-stage (2 for seven digits) ring, one thread of warp 21 issues tcgen05.mma
+// (cta_group::1, kind::f16, 128 x 80 x 16) into TMEM, warps 0-19 drain TMEM
+// (tcgen05.ld, five warps per 32-lane quadrant, 16 columns each) and write
+// the output.  Every wait is bounded; on expiry the
 // kernel records an error, waits (bounded) for its in-flight copies and MMAs,
 // frees its TMEM and returns.
 #include <cuda.h>
@@ -55,12 +56,16 @@ __device__ __forceinline__ int acc_of_level(int L) { return L < MAX_ACC - 1 ? L 
 __host__ __device__ inline uint32_t tmem_pow2(uint32_t c) {
   return c <= 32 ? 32u : (c <= 64 ? 64u : (c <= 128 ? 128u : (c <= 256 ? 256u : 512u)));
 }
-// Warps 0-7 epilogue (two per TMEM lane quadrant, each half of the tile's
-// columns), warp 8 producer, warp 9 MMA.
-constexpr int NT = 320;
-constexpr int NEPI = 256;
-constexpr int PRODUCER_WARP = 8, MMA_WARP = 9;
-constexpr int EPI_COLS = TN / 2;  // columns per epilogue thread
+// Warps 0-19 epilogue (five per TMEM lane quadrant, each a fifth of the
+// tile's columns), warp 20 producer, warp 21 MMA.  The epilogue is latency-
+// bound (FP64 adds, C loads, TMEM loads): five warps per quadrant instead of
+// two hide it -- 257 -> 206 ms of tensor-phase time per 16384^2 mixed
+// factorization -- at 80 registers per thread.
+constexpr int NT = 704;
+constexpr int NEPI = 640;
+constexpr int PRODUCER_WARP = 20, MMA_WARP = 21;
+constexpr int EPI_COLS = TN / 5;  // columns per epilogue thread (a multiple of 8)
+static_assert(TN % 5 == 0 && EPI_COLS % 8 == 0, "epilogue columns come in TMEM loads of 8");
 constexpr int A_TILE = TM * TK * 2;  // 8 KB per digit tile
 constexpr int B_TILE = TN * TK * 2;  // 5 KB per digit tile
 
@@ -696,7 +701,7 @@ __global__ void __launch_bounds__(NT, 1) ozk_gemm_kernel(OzkArgs a,
       mma_commit(&done_bar);
     }
   } else {
-    // Epilogue warps 0-7: TMEM lanes 32*(warp&3).. = tile rows, columns
+    // Epilogue warps 0-19: TMEM lanes 32*(warp&3).. = tile rows, columns
     // (warp>>2)*EPI_COLS.. of the tile.
     float hi[EPI_COLS], lo[EPI_COLS];
 #pragma unroll
