@@ -223,6 +223,26 @@ class ClockSampler:
 # CPU baseline: the oracle (restatement of the reference, LAPACK/BLAS from
 # scipy's OpenBLAS) on the host cores.
 
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo), for the
+    cpu_baseline record; 'unknown' if neither says."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().lower().startswith("model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
 def cpu_oracle_run(n, nb, pp, reps, seed):
     import oracle
     try:
@@ -270,7 +290,7 @@ def run_reference_arm(args):
             "config": {"workload": "HQRRP m=n=%d nb=%d pp=%d, reference algorithm on host cores"
                        % (n, args.nb, args.pp), "m": n, "n": n, "nb": args.nb, "pp": args.pp},
             "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": cores, "kind": kind,
-                             "sample": sample},
+                             "sample": sample, "cpu_model": cpu_model()},
             "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -564,6 +584,7 @@ def cpu_batched_run(shapes, offs, flat0, stride=1, reps=3):
             sec = min(sec, time.perf_counter() - t0)
     fl = sum(flops_qr(*shapes[i]) for i in idx)
     return {"value": fl / sec / 1e12, "unit": "TFLOP/s", "cores": cores, "kind": kind,
+            "cpu_model": cpu_model(),
             "sample": "dgeqp4 (-> LAPACK dgeqpf/dgeqp3) on %d of the %d matrices, %d threads "
                       "x 1 BLAS thread, best of %d: %.2f s" % (len(idx), len(shapes), cores,
                                                               reps, sec)}
@@ -730,7 +751,7 @@ def main():
         t = min(times)
         t3 = cpu_dgeqp3_run(args.cpu_n, args.seed)
         cpu = {"value": flops_qr(args.cpu_n, args.cpu_n) / t / 1e12, "unit": "TFLOP/s",
-               "cores": cores, "kind": kind,
+               "cores": cores, "kind": kind, "cpu_model": cpu_model(),
                "sample": "HQRRP nb=%d pp=%d on m=n=%d, same spectrum as the square workload, "
                          "best of 2, %.1f s each" % (nb, pp, args.cpu_n, t),
                "lapack_dgeqp3": {"value": flops_qr(args.cpu_n, args.cpu_n) / t3 / 1e12,

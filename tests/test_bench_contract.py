@@ -39,6 +39,7 @@ def test_reference_arm_line():
     assert abs(d["value"] - flops / (d["ms_per_step"] * 1e-3) / 1e12) <= 1e-6 * d["value"]
     cb = d["cpu_baseline"]
     assert cb["value"] == d["value"] and cb["kind"] in ("reference", "port") and cb["cores"] >= 1
+    assert isinstance(cb["cpu_model"], str) and cb["cpu_model"]
     e2e = d["e2e"]
     assert e2e["value"] == d["value"] and e2e["unit"] == d["unit"]
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
