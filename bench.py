@@ -133,6 +133,23 @@ def make_matrix_cpu(n, seed):
     return oracle.with_spectrum(n, n, spectrum(n), seed)
 
 
+def make_batched_gpu(shapes, seed, device):
+    """The batched workload's matrices A_i = U diag(i^-2) V^T (Haar U, V),
+    column-major, back to back in one flat FP64 buffer; returns (flat, offsets)."""
+    import torch
+    _preload_linalg()
+    sizes = [m * n for m, n in shapes]
+    offs = np.concatenate([[0], np.cumsum(sizes)]).astype(int)
+    flat = torch.empty(max(1, int(offs[-1])), dtype=torch.float64, device=device)
+    g = torch.Generator(device=device).manual_seed(seed)
+    for i, (m, n) in enumerate(shapes):
+        k = min(m, n)
+        U, V = _orth(m, k, g, device), _orth(n, k, g, device)
+        sig = (1.0 + torch.arange(k, dtype=torch.float64, device=device)) ** -2.0
+        flat[offs[i]:offs[i + 1]].view(n, m).copy_((V * sig[None, :]) @ U.T)
+    return flat, offs
+
+
 def batched_shapes(count, seed):
     """m log-uniform in [64, 1024], n log-uniform in [32, min(m, 512)]."""
     rng = np.random.default_rng(seed)
@@ -428,16 +445,7 @@ def run_batched(hq, args, device, dist, rank, world, local):
     mine = shard.partition_by_cost(shapes_all, world)[rank] if world > 1 else list(
         range(len(shapes_all)))
     shapes = [shapes_all[i] for i in mine]
-    flops = sum(flops_qr(m, n) for m, n in shapes)
-    sizes = [m * n for m, n in shapes]
-    offs = np.concatenate([[0], np.cumsum(sizes)]).astype(int)
-    flat0 = torch.empty(int(offs[-1]), dtype=torch.float64, device=device)
-    g = torch.Generator(device=device).manual_seed(args.seed + 1000 * rank)
-    for i, (m, n) in enumerate(shapes):
-        k = min(m, n)
-        U, V = _orth(m, k, g, device), _orth(n, k, g, device)
-        sig = (1.0 + torch.arange(k, dtype=torch.float64, device=device)) ** -2.0
-        flat0[offs[i]:offs[i + 1]].view(n, m).copy_((V * sig[None, :]) @ U.T)
+    flat0, offs = make_batched_gpu(shapes, args.seed + 1000 * rank, device)
     flat = flat0.clone()
     mats = [flat[offs[i]:offs[i + 1]].view(n, m) for i, (m, n) in enumerate(shapes)]
     torch.cuda.synchronize()

@@ -45,6 +45,9 @@ def load():
     L = C.CDLL(LIB_PATH, mode=C.RTLD_LOCAL)
     L.dgeqp4.argtypes = [_ip, _ip, _dp, _ip, _ip, _dp, _dp, _ip, _ip]
     L.dgeqp4.restype = None
+    L.hqrrp_gb300_dgeqp4_sketch.argtypes = [_ip, _ip, _dp, _ip, _ip, _dp, _dp, _ip, _ip, _dp,
+                                            C.c_int]
+    L.hqrrp_gb300_dgeqp4_sketch.restype = None
     L.NoFLA_HQRRP_WY_blk_var4.argtypes = [C.c_int, C.c_int, _dp, C.c_int, _ip, _dp, C.c_int,
                                           C.c_int, C.c_int]
     L.NoFLA_HQRRP_WY_blk_var4.restype = C.c_int
@@ -64,12 +67,17 @@ def load():
     L.hqrrp_gb300_dgeqp4_device.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p,
                                             C.c_void_p, C.c_void_p]
     L.hqrrp_gb300_dgeqp4_device.restype = C.c_int
+    L.hqrrp_gb300_sketch_device.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_int,
+                                            C.c_ulonglong, C.c_void_p]
+    L.hqrrp_gb300_sketch_device.restype = C.c_int
     L.hqrrp_gb300_profile_enable.argtypes = [C.c_int]
     L.hqrrp_gb300_profile_enable.restype = None
     L.hqrrp_gb300_profile_read.argtypes = [_dp, _dp, C.c_int]
     L.hqrrp_gb300_profile_read.restype = C.c_int
     L.hqrrp_gb300_launch_count.argtypes = []
     L.hqrrp_gb300_launch_count.restype = C.c_ulonglong
+    L.hqrrp_gb300_pool_alloc_count.argtypes = []
+    L.hqrrp_gb300_pool_alloc_count.restype = C.c_ulonglong
     L.hqrrp_gb300_ozaki_dgemm.argtypes = [C.c_char, C.c_char, C.c_int, C.c_int, C.c_int,
                                           C.c_double, C.c_void_p, C.c_int, C.c_void_p, C.c_int,
                                           C.c_double, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
@@ -161,6 +169,11 @@ def launch_count():
     return int(load().hqrrp_gb300_launch_count())
 
 
+def pool_alloc_count():
+    """Device allocations the library has made from its memory pools."""
+    return int(load().hqrrp_gb300_pool_alloc_count())
+
+
 def _fortran(A):
     return np.array(np.asarray(A, dtype=np.float64), order="F", copy=True)
 
@@ -190,10 +203,12 @@ def hqrrp(A, nb=64, pp=10, panel_pivoting=1, jpvt=None, G=None):
     return A, jp, tau[:min(m, n)]
 
 
-def dgeqp4(A, jpvt=None, lwork=None):
+def dgeqp4(A, jpvt=None, lwork=None, G=None):
     """dgeqp4 on a copy of A; returns (A_out, jpvt, tau, info, work0).
 
-    info < 0 is an argument error (as LAPACK); info > 1000 raises."""
+    G: optional explicit sketch of the HQRRP branch (74 x m, the first m - nf
+    columns read; hqrrp_gb300_dgeqp4_sketch).  info < 0 is an argument error
+    (as LAPACK); info > 1000 raises."""
     L = load()
     A = _fortran(A)
     m, n = A.shape
@@ -205,9 +220,17 @@ def dgeqp4(A, jpvt=None, lwork=None):
     work = np.zeros(max(1, lwork), dtype=np.float64)
     mi, ni, ldi, lw, info = (C.c_int(m), C.c_int(n), C.c_int(max(1, m)), C.c_int(lwork),
                              C.c_int(0))
-    L.dgeqp4(C.byref(mi), C.byref(ni), A.ctypes.data_as(_dp), C.byref(ldi),
-             jp.ctypes.data_as(_ip), tau.ctypes.data_as(_dp), work.ctypes.data_as(_dp),
-             C.byref(lw), C.byref(info))
+    args = (C.byref(mi), C.byref(ni), A.ctypes.data_as(_dp), C.byref(ldi),
+            jp.ctypes.data_as(_ip), tau.ctypes.data_as(_dp), work.ctypes.data_as(_dp),
+            C.byref(lw), C.byref(info))
+    if G is None:
+        L.dgeqp4(*args)
+    else:
+        Gf = np.zeros((74, max(1, m)), order="F")
+        g = np.asarray(G, dtype=np.float64)
+        assert g.shape[0] == 74 and g.shape[1] <= m
+        Gf[:, :g.shape[1]] = g
+        L.hqrrp_gb300_dgeqp4_sketch(*args, Gf.ctypes.data_as(_dp), 74)
     if info.value > 1000:
         raise HQRRPError("dgeqp4 failed (info=%d): %s" % (info.value, last_error()))
     return A, jp, tau[:min(m, n)], info.value, work[0]
@@ -235,6 +258,17 @@ def hqrrp_device(At, jpvt, tau, nb=64, pp=10, panel_pivoting=1, Gt=None, seed=12
                                     nb + pp, int(seed), _stream_ptr(stream))
     if rc != 0:
         raise HQRRPError("hqrrp_device failed (%d): %s" % (rc, last_error()))
+
+
+def sketch_device(rows, cols, seed=12, stream=None):
+    """The device Philox sketch ((cols, rows) contiguous = column-major rows x cols)."""
+    import torch
+    Gt = torch.empty((cols, rows), dtype=torch.float64, device="cuda")
+    rc = load().hqrrp_gb300_sketch_device(rows, cols, Gt.data_ptr(), rows, int(seed),
+                                          _stream_ptr(stream))
+    if rc != 0:
+        raise HQRRPError("sketch_device failed (%d): %s" % (rc, last_error()))
+    return Gt
 
 
 def dgeqp4_device(At, jpvt, tau, stream=None):

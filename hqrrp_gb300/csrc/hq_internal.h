@@ -22,6 +22,7 @@ extern "C" {
 /* Limits of the kernels. */
 #define HQ_MAX_MY 256    /* nb + pp (rows of the sketch) */
 #define HQ_MAX_PANEL 1024 /* columns of one pivoted panel kernel */
+#define HQ_WIDE_MAX_ROWS 1024 /* rows of the wide pivoted QR kernel */
 
 typedef struct hq_device_info {
   int device;
@@ -72,6 +73,16 @@ size_t hq_panel_part_elems(const hq_device_info* dev, int nc);
 #define HQ_PANEL_PART_ELEMS(ctas, nc) \
   (2 * (size_t)(ctas) * (size_t)(((nc) + 2) & ~1) + \
    3 * (size_t)HQ_PANEL_FX_CS * (size_t)(((nc) + 2) & ~1))
+
+/* ---- Wide pivoted QR: m <= HQ_WIDE_MAX_ROWS rows, any number of columns --
+ * dgeqp3's result for an m x n matrix A (lda), in place except for the
+ * column order: the final order is written as (dst, src) pairs (at most
+ * 2 min(m, n) of them, count in *npairs) for hq_permute_pairs.  phys: n ints;
+ * cand: hq_wide_cand_elems(dev) 64-bit words. */
+size_t hq_wide_cand_elems(const hq_device_info* dev);
+int hq_wide_qrp(cudaStream_t stream, const hq_device_info* dev, int m, int n, double* A, int lda,
+                double* tau, int* phys, long long* cand, int* pairs, int* npairs, unsigned* bar,
+                int* err, unsigned spin_limit);
 
 /* ---- T factor of a forward columnwise block reflector (DLARFT) -----------
  * Z = U^T U (k x k, ldz) is given; writes T (k x k, ldt), zero below the

@@ -14,8 +14,16 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "hq_internal.h"
 #include "hqrrp_gb300.h"
+
+/* NVTX ranges around the phases of every call (header-only NVTX v3: a no-op
+ * unless a tool such as Nsight Systems is attached).  The ranges cover the
+ * host's enqueueing; the tool attributes the kernels launched inside them. */
+#define NV_PUSH(name) nvtxRangePushA(name)
+#define NV_POP() nvtxRangePop()
 
 #define HQ_API __attribute__((visibility("default")))
 
@@ -28,6 +36,8 @@ enum {
 };
 
 #define DGEQP4_SMALL_DGEQP3 1000 /* ...var4.c:58 */
+#define DGEQP4_NB 64 /* HQRRP block size and oversampling dgeqp4 uses (...var4.c:264) */
+#define DGEQP4_PP 10
 #define LAPACK_NB_DGEQRF 32 /* ILAENV(1, 'DGEQRF') of reference LAPACK */
 #define FIXED_BLOCK 128
 #define DEFAULT_SPIN_LIMIT (1u << 22)
@@ -160,6 +170,7 @@ typedef struct {
   cudaStream_t st;
   void* ptrs[MAX_ALLOCS];
   int nptr;
+  int nalloc; /* allocations attempted by this call */
   int failed;
   /* HQRRP buffers */
   double *G, *Y, *V, *U, *T, *Z, *W1, *W2, *Bm, *B2, *ws, *part, *rowbuf, *tmp;
@@ -254,10 +265,36 @@ HQ_API int hqrrp_gb300_profile_counts(int* counts, int n) {
 
 HQ_API unsigned long long hqrrp_gb300_launch_count(void) { return hq_launches(); }
 
+/* Device allocations made from the library's pools since the process
+ * started. */
+static unsigned long long g_pool_allocs = 0;
+
+HQ_API unsigned long long hqrrp_gb300_pool_alloc_count(void) {
+  return __atomic_load_n(&g_pool_allocs, __ATOMIC_RELAXED);
+}
+
+/* Host-side fault injection: HQRRP_GB300_FAIL_ALLOC=k (k >= 1) makes the k-th
+ * device allocation of every call fail as if the pool were out of memory, so
+ * the error path (return code / info 1000 + 4, message, workspace released)
+ * can be exercised without a GPU fault.  Unset or 0: off. */
+static int injected_alloc_failure(hq_ws* w) {
+  const char* e = getenv("HQRRP_GB300_FAIL_ALLOC");
+  if (!e || !*e) return 0;
+  const long k = strtol(e, NULL, 10);
+  return k > 0 && (long)w->nalloc == k;
+}
+
 static void* ws_alloc(hq_ws* w, size_t bytes) {
   void* p = NULL;
   if (w->failed) return NULL;
   if (bytes == 0) bytes = 16;
+  w->nalloc++;
+  if (injected_alloc_failure(w)) {
+    set_err("device allocation of %zu bytes failed: injected by HQRRP_GB300_FAIL_ALLOC=%d",
+            bytes, w->nalloc);
+    w->failed = 1;
+    return NULL;
+  }
   cudaError_t e = cudaMallocFromPoolAsync(&p, bytes, w->ds->pool, w->st);
   if (e != cudaSuccess || w->nptr >= MAX_ALLOCS) {
     set_err("device allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
@@ -265,6 +302,7 @@ static void* ws_alloc(hq_ws* w, size_t bytes) {
     return NULL;
   }
   w->ptrs[w->nptr++] = p;
+  __atomic_add_fetch(&g_pool_allocs, 1ULL, __ATOMIC_RELAXED);
   return p;
 }
 
@@ -593,6 +631,7 @@ static int core_hqrrp_k(hq_ws* w, int m, int n, double* dA, int ldda, int* djpvt
   if (mn == 0) return HQ_OK;
 
   /* Sketch G and Y = G A. */
+  NV_PUSH("hqrrp.sketch");
   if (dG) CK(hq_copy_matrix(w->st, mY, m, dG, lddg, w->G, w->ldg));
   else CK(hq_sketch_philox(w->st, mY, m, w->G, w->ldg, seed));
   if (w->mixed) {
@@ -605,6 +644,7 @@ static int core_hqrrp_k(hq_ws* w, int m, int n, double* dA, int ldda, int* djpvt
     DG('N', 'N', mY, n, m, 1.0, w->G, w->ldg, dA, ldda, 0.0, w->Y, w->ldy);
     prof_mark(w, PH_SKETCH, 2.0 * mY * m * n);
   }
+  NV_POP();
 
   int cx_ok = 0; /* w->colexp holds the trailing columns' exponent fields */
   for (int j = 0; j < mn; j += nb) {
@@ -616,7 +656,9 @@ static int core_hqrrp_k(hq_ws* w, int m, int n, double* dA, int ldda, int* djpvt
     double* ABR = AR + j;
     double* YR = w->Y + (size_t)j * w->ldy;
 
+    NV_PUSH("hqrrp.block");
     if (!last) {
+      NV_PUSH("hqrrp.select");
       /* Pivot selection on the sketch, then one gather of A, Y and jpvt. */
       /* Mixed: the sketch's reflector applications in FP32 (it is formed from
        * two-digit BF16 operands and only steers pivots); norms stay FP64. */
@@ -629,8 +671,10 @@ static int core_hqrrp_k(hq_ws* w, int m, int n, double* dA, int ldda, int* djpvt
       double fl = 0.0;
       for (int s2 = 0; s2 < b; ++s2) fl += 4.0 * (mY - s2) * (n - j - s2 - 1);
       prof_mark(w, PH_SELECT, fl);
+      NV_POP();
     }
 
+    NV_PUSH("hqrrp.panel");
     /* Panel QR (pivoted within its b columns), U, tau. */
     /* Mixed: squared column norms in the panel's pivoting (division-free
      * LAWN 176 downdate); plain keeps LAPACK's formula. */
@@ -649,15 +693,19 @@ static int core_hqrrp_k(hq_ws* w, int m, int n, double* dA, int ldda, int* djpvt
       for (int s2 = 0; s2 < b; ++s2) fl += 4.0 * (mp - s2) * (b - s2 - 1);
       prof_mark(w, PH_PANEL, fl);
     }
+    NV_POP();
 
     /* T and the trailing update [A12; A22] := Q^T [A12; A22]. */
     int* cx_out = (w->mixed && w->colexp && nc2 > 0) ? w->colexp + j + b : NULL;
+    NV_PUSH("hqrrp.update");
     int rc = block_reflector(w, mp, b, dtau + j, ABR + (size_t)b * ldda, ldda, nc2,
                              cx_ok ? w->colexp + j + b : NULL, cx_out);
+    NV_POP();
     if (rc) return rc;
     cx_ok = cx_out != NULL;
 
     if (!last && !(final_block && mn < imin(m, n))) {
+      NV_PUSH("hqrrp.downdate");
       /* Sketch downdate (...var4.c:617-708):
        *   G_R := G_R (I - U T U^T);  Y2 -= G_R[:, 0:b] R12. */
       double* GR = w->G + (size_t)j * w->ldg;
@@ -689,7 +737,9 @@ static int core_hqrrp_k(hq_ws* w, int m, int n, double* dA, int ldda, int* djpvt
            YR + (size_t)b * w->ldy, w->ldy);
         prof_mark(w, PH_DOWNDATE, 4.0 * mY * mp * b + 2.0 * mY * b * b + 2.0 * mY * b * nc2);
       }
+      NV_POP();
     }
+    NV_POP();
   }
   return HQ_OK;
 }
@@ -824,6 +874,25 @@ HQ_API int hqrrp_gb300_hqrrp_device(int m, int n, double* dA, int ldda, int* d_j
   return rc;
 }
 
+HQ_API int hqrrp_gb300_sketch_device(int rows, int cols, double* dG, int ldg,
+                                    unsigned long long seed, void* stream) {
+  g_err[0] = 0;
+  if (rows < 0 || cols < 0 || ldg < imax(1, rows)) {
+    set_err("hqrrp_gb300_sketch_device: invalid rows, cols or ldg");
+    return HQ_E_UNSUPPORTED;
+  }
+  if (rows == 0 || cols == 0) return 0;
+  if (!current_device()) return HQ_E_CUDA;
+  cudaStream_t st = (cudaStream_t)stream;
+  int e = hq_sketch_philox(st, rows, cols, dG, ldg, seed);
+  if (!e) e = (int)cudaStreamSynchronize(st);
+  if (e) {
+    set_err("hqrrp_gb300_sketch_device: %s", cudaGetErrorString((cudaError_t)e));
+    return HQ_E_CUDA;
+  }
+  return 0;
+}
+
 /* ------------------------------------------------------------------------ */
 /* dgeqp4 (...var4.c:127-300) on device data.                                */
 
@@ -856,8 +925,10 @@ static int fixed_columns_front(int n, int* hjp, int* src) {
 /* Everything of dgeqp4 after argument checking.  hjp: host copy of jpvt (in:
  * fixed marks; out: 1-based permutation).  Returns HQ_* and the LAPACK-style
  * workspace figure in *iws_out. */
+/* dG (optional, lddg >= 74): the sketch of the HQRRP branch, 74 x (m - nf)
+ * (its first m - nf columns are read); NULL draws Philox(seed). */
 static int core_dgeqp4(hq_ws* w, int m, int n, double* dA, int ldda, int* hjp, int* djp,
-                       double* dtau, int* iws_out) {
+                       double* dtau, int* iws_out, const double* dG, int lddg) {
   const hq_device_info* dev = &w->ds->dev;
   const int mn = imin(m, n);
   const int small = mn < DGEQP4_SMALL_DGEQP3;
@@ -934,18 +1005,30 @@ static int core_dgeqp4(hq_ws* w, int m, int n, double* dA, int ldda, int* hjp, i
     const int mt = m - nf, nt = n - nf;
     double* At = dA + nf + (size_t)nf * ldda;
     CK(hq_fill_iota(w->st, w->labels, nt, 0));
-    if (small) {
-      if (nt > HQ_MAX_PANEL) {
-        set_err("dgeqp4 small-matrix path supports at most %d free columns (got %d)",
-                HQ_MAX_PANEL, nt);
-        return HQ_E_UNSUPPORTED;
-      }
+    if (small && nt > HQ_MAX_PANEL) {
+      /* Wide: min(m, n) < 1000 and more than HQ_MAX_PANEL free columns, so
+       * mt < 1000 rows.  The column-partitioned kernel leaves the columns in
+       * place and reports the final order as pairs, applied here to all m
+       * rows of the free columns (the rows above them included) and to jpvt. */
+      const int ns = imin(mt, nt);
+      int* phys = ws_alloc(w, sizeof(int) * (size_t)nt);
+      long long* cand = ws_alloc(w, sizeof(long long) * hq_wide_cand_elems(dev));
+      int* wpairs = ws_alloc(w, sizeof(int) * 4 * (size_t)ns);
+      int* wlab = ws_alloc(w, sizeof(int) * 2 * (size_t)ns);
+      double* wtmp = ws_alloc(w, sizeof(double) * (size_t)m * 2 * ns);
+      if (w->failed) return HQ_E_NOMEM;
+      CK(hq_wide_qrp(w->st, dev, mt, nt, At, ldda, dtau + nf, phys, cand, wpairs, w->npairs,
+                     w->bar + 1, w->err, spin));
+      CK(hq_permute_pairs(w->st, m, dA + (size_t)nf * ldda, ldda, nt, wpairs, w->npairs, 2 * ns,
+                          wtmp, djp + nf, wlab));
+    } else if (small) {
       CK(hq_panel_qrp(w->st, dev, mt, nt, 1, At, ldda, dtau + nf, NULL, w->ldu, w->perm,
                       w->part, w->part_elems, w->rowbuf, w->bar + 1, w->err, spin, 0));
       CK(hq_permute_cols(w->st, nf, dA + (size_t)nf * ldda, ldda, nt, w->perm, w->tmp,
                          djp + nf, w->label_tmp));
     } else {
-      int rc = core_hqrrp(w, mt, nt, At, ldda, w->labels, dtau + nf, 64, 10, 1, NULL, 0, g_seed);
+      int rc = core_hqrrp(w, mt, nt, At, ldda, w->labels, dtau + nf, DGEQP4_NB, DGEQP4_PP, 1, dG,
+                          lddg, g_seed);
       if (rc) return rc;
       double* t2 = w->tmp;
       if ((size_t)nf * nt > (size_t)w->tmp_rows * w->tmp_cols) {
@@ -969,7 +1052,7 @@ static int dgeqp4_ws(hq_ws* w, int m, int n) {
     int rc = ws_setup(w, m, n, 0, 0, imax(FIXED_BLOCK, imin(n, HQ_MAX_PANEL)));
     return rc;
   }
-  return ws_setup(w, m, n, 64, 10, FIXED_BLOCK);
+  return ws_setup(w, m, n, DGEQP4_NB, DGEQP4_PP, FIXED_BLOCK);
 }
 
 static void xerbla_dgeqp3(int arg) {
@@ -1000,11 +1083,14 @@ static int dgeqp4_prologue(int m, int n, int lda, int lwork, double* work, int* 
   return query || mn == 0;
 }
 
-HQ_API void dgeqp4(int* m, int* n, double* A, int* lda, int* jpvt, double* tau, double* work,
-                   int* lwork, int* info) {
+/* Host-pointer dgeqp4; G (optional, ldg >= 74, m columns of which the first
+ * m - nf are read) replaces the drawn sketch of the HQRRP branch. */
+static void dgeqp4_host(int* m, int* n, double* A, int* lda, int* jpvt, double* tau,
+                        double* work, int* lwork, int* info, const double* G, int ldg) {
   g_err[0] = 0;
   if (dgeqp4_prologue(*m, *n, *lda, *lwork, work, info)) return;
   const int M = *m, N = *n, LDA = *lda, mn = imin(M, N), ldda = round_up(M, 32);
+  const int mY = DGEQP4_NB + DGEQP4_PP;
   hq_ws w;
   int rc = ws_begin(&w, NULL, 0);
   if (rc) {
@@ -1016,14 +1102,19 @@ HQ_API void dgeqp4(int* m, int* n, double* A, int* lda, int* jpvt, double* tau, 
   double* dA = rc ? NULL : ws_alloc(&w, sizeof(double) * (size_t)ldda * N);
   double* dtau = rc ? NULL : ws_alloc(&w, sizeof(double) * (size_t)mn);
   int* djp = rc ? NULL : ws_alloc(&w, sizeof(int) * (size_t)N);
+  double* dG = (rc || !G || mn < DGEQP4_SMALL_DGEQP3) ? NULL
+                                                      : ws_alloc(&w, sizeof(double) * (size_t)mY * M);
   if (!rc && w.failed) rc = HQ_E_NOMEM;
   cudaStream_t st = w.st;
   if (hjp) memcpy(hjp, jpvt, sizeof(int) * (size_t)N);
   CKF(cudaMemcpy2DAsync(dA, sizeof(double) * ldda, A, sizeof(double) * LDA, sizeof(double) * M, N,
                         cudaMemcpyHostToDevice, st));
+  if (dG)
+    CKF(cudaMemcpy2DAsync(dG, sizeof(double) * mY, G, sizeof(double) * ldg, sizeof(double) * mY,
+                          M, cudaMemcpyHostToDevice, st));
   int iws = 3 * N + 1;
   if (!rc) drain_begin(&w, A, LDA, dA, ldda, M);
-  if (!rc) rc = core_dgeqp4(&w, M, N, dA, ldda, hjp, djp, dtau, &iws);
+  if (!rc) rc = core_dgeqp4(&w, M, N, dA, ldda, hjp, djp, dtau, &iws, dG, mY);
   if (!rc) rc = drain_finish(&w, A, LDA, dA, ldda, M, N);
   if (!rc) rc = ws_check(&w);
   CKF(cudaMemcpyAsync(jpvt, djp, sizeof(int) * N, cudaMemcpyDeviceToHost, st));
@@ -1036,6 +1127,23 @@ HQ_API void dgeqp4(int* m, int* n, double* A, int* lda, int* jpvt, double* tau, 
     return;
   }
   work[0] = (double)iws;
+}
+
+HQ_API void dgeqp4(int* m, int* n, double* A, int* lda, int* jpvt, double* tau, double* work,
+                   int* lwork, int* info) {
+  dgeqp4_host(m, n, A, lda, jpvt, tau, work, lwork, info, NULL, 0);
+}
+
+HQ_API void hqrrp_gb300_dgeqp4_sketch(int* m, int* n, double* A, int* lda, int* jpvt,
+                                      double* tau, double* work, int* lwork, int* info,
+                                      const double* G, int ldg) {
+  if (G == NULL || ldg < DGEQP4_NB + DGEQP4_PP) {
+    g_err[0] = 0;
+    set_err("hqrrp_gb300_dgeqp4_sketch: sketch missing or ldg < %d", DGEQP4_NB + DGEQP4_PP);
+    *info = 1000 + HQ_E_UNSUPPORTED;
+    return;
+  }
+  dgeqp4_host(m, n, A, lda, jpvt, tau, work, lwork, info, G, ldg);
 }
 
 HQ_API int hqrrp_gb300_dgeqp4_device(int m, int n, double* dA, int ldda, int* d_jpvt,
@@ -1053,7 +1161,7 @@ HQ_API int hqrrp_gb300_dgeqp4_device(int m, int n, double* dA, int ldda, int* d_
   CKF(cudaMemcpyAsync(hjp, d_jpvt, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
   CKF(cudaStreamSynchronize(st));
   int iws = 0;
-  if (!rc) rc = core_dgeqp4(&w, m, n, dA, ldda, hjp, d_jpvt, d_tau, &iws);
+  if (!rc) rc = core_dgeqp4(&w, m, n, dA, ldda, hjp, d_jpvt, d_tau, &iws, NULL, 0);
   if (!rc) rc = ws_check(&w);
   ws_release(&w);
   CKF(cudaStreamSynchronize(st));

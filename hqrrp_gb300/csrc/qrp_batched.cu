@@ -61,8 +61,11 @@ __global__ void __launch_bounds__(NT) qrp_batched_kernel(BatchArgs a) {
     if (item < 0) break;
     const int m = a.m[item], n = a.n[item], lda = a.lda[item];
     double* Ag = a.A[item];
-    if (m <= 0 || n <= 0 || n > a.max_n || lda < max(1, m)) {
-      if (tid == 0 && a.info) a.info[item] = (n > a.max_n) ? HQ_ERR_BAD_SHAPE : 0;
+    // A size the kernel cannot take (negative, lda < max(1, m), more than
+    // max_n columns) is flagged and left untouched; an empty matrix is done.
+    const bool bad = m < 0 || n < 0 || n > a.max_n || lda < max(1, m);
+    if (bad || m == 0 || n == 0) {
+      if (tid == 0 && a.info) a.info[item] = bad ? HQ_ERR_BAD_SHAPE : 0;
       continue;
     }
     const bool staged = (long long)m * n * 8 <= a.stage_bytes;

@@ -84,6 +84,17 @@ void hqrrp_gb300_set_spin_limit(unsigned limit);
 int hqrrp_gb300_hqrrp_sketch(int m, int n, double* A, int lda, int* jpvt, double* tau,
                              int nb, int pp, int panel_pivoting, const double* G, int ldg);
 
+/* dgeqp4 with an explicit host sketch for its HQRRP branch (min(m,n) >= 1000):
+ * G is 74 x m ((64 + 10) rows, leading dimension ldg >= 74) and its first
+ * m - nf columns (nf = number of fixed columns, at most m) replace the sketch
+ * the reference draws inside NoFLA_HQRRP_WY_blk_var4 for the free block
+ * (lapack_compatible_sources/NoFLA_HQRRP_WY_blk_var4.c:257-265).  Everything
+ * else is dgeqp4 above; the small-matrix branches do not read G.  With the
+ * reference's own sketch of the free block this reproduces the reference's
+ * dgeqp4 up to rounding.  info = 1003 if G is NULL or ldg < 74. */
+void hqrrp_gb300_dgeqp4_sketch(int* m, int* n, double* A, int* lda, int* jpvt, double* tau,
+                               double* work, int* lwork, int* info, const double* G, int ldg);
+
 /* Device-pointer HQRRP on `stream` (a cudaStream_t, NULL = legacy default).
  * dA (ldda >= m), d_jpvt (n ints, carried), d_tau (min(m,n)).  dG: optional
  * device sketch ((nb+pp) x m, lddg); NULL draws Philox(seed).  Blocks until
@@ -91,6 +102,17 @@ int hqrrp_gb300_hqrrp_sketch(int m, int n, double* A, int lda, int* jpvt, double
 int hqrrp_gb300_hqrrp_device(int m, int n, double* dA, int ldda, int* d_jpvt, double* d_tau,
                              int nb, int pp, int panel_pivoting, const double* dG, int lddg,
                              unsigned long long seed, void* stream);
+
+/* The Gaussian sketch the factorization draws when none is supplied: dG
+ * (rows x cols, column-major, ldg >= rows) on the device, element e = c*rows + r
+ * from Philox4x32-10 (Salmon et al., SC'11) of counter e / 2 under key =
+ * seed, its 128 bits turned into two N(0,1) values by Box-Muller (even e the
+ * cosine branch, odd e the sine branch).  Replaces the reference's polar
+ * method over libc rand() (lapack_compatible_sources/
+ * NoFLA_HQRRP_WY_blk_var4.c:575-614) as a counter-based generator.  Blocks
+ * until done; returns 0 or an error code. */
+int hqrrp_gb300_sketch_device(int rows, int cols, double* dG, int ldg, unsigned long long seed,
+                              void* stream);
 
 /* Device-pointer dgeqp4 (same semantics as dgeqp4; jpvt/tau on the device,
  * no work array).  Returns info. */
@@ -194,6 +216,14 @@ int hqrrp_gb300_profile_counts(int* counts, int n);
 
 /* Number of kernels this library has launched in this process. */
 unsigned long long hqrrp_gb300_launch_count(void);
+
+/* Number of device allocations this library has made from its memory pools
+ * in this process (every entry point except hqrrp_gb300_qrp_noalloc draws its
+ * workspace from a pool).  Setting HQRRP_GB300_FAIL_ALLOC=k in the
+ * environment makes the k-th allocation of every later call fail as if the
+ * device were out of memory (return code 4, dgeqp4 info 1004): host-side
+ * fault injection for testing callers' error paths. */
+unsigned long long hqrrp_gb300_pool_alloc_count(void);
 
 /* Message of the last failure on the calling thread ("" if none). */
 const char* hqrrp_gb300_last_error(void);

@@ -127,6 +127,9 @@ class Oracle(_Base):
             g = getattr(self.lib, name)
             g.argtypes = [_ip, _ip, _dp, _ip, _ip, _dp, _dp, _ip, _ip]
         self.lib.oracle_dgeqpf.argtypes = [_ip, _ip, _dp, _ip, _ip, _dp, _dp, _ip]
+        self.lib.oracle_dgeqp4_sketch.argtypes = [_ip, _ip, _dp, _ip, _ip, _dp, _dp, _ip, _ip,
+                                                  _dp, C.c_int]
+        self.lib.oracle_dgeqp4_sketch.restype = None
         self.lib.oracle_set_threads.argtypes = [C.c_int]
 
     def set_threads(self, n):
@@ -144,6 +147,25 @@ class Oracle(_Base):
         self._hqrrp_sketch(m, n, _dptr(A), max(1, m), _iptr(jp), _dptr(tau), nb, pp,
                            panel_pivoting, _dptr(G), nb + pp)
         return A, jp, tau[:min(m, n)]
+
+    def dgeqp4_sketch(self, A, G, jpvt=None):
+        """dgeqp4 whose HQRRP branch uses the sketch G (74 x (m - nf)) in place of
+        the drawn one; returns (A_out, jpvt, tau, info, work0)."""
+        A = _fortran(A)
+        G = _fortran(G)
+        m, n = A.shape
+        assert G.shape[0] == 74
+        jp = (np.zeros(n, dtype=np.int32) if jpvt is None
+              else np.array(jpvt, dtype=np.int32, copy=True))
+        tau = np.zeros(max(1, min(m, n)), dtype=np.float64)
+        lwork = max(1, 3 * n + 1, 2 * n + (n + 1) * 64)
+        work = np.zeros(lwork, dtype=np.float64)
+        mi, ni, ldi, lw, info = (C.c_int(m), C.c_int(n), C.c_int(max(1, m)), C.c_int(lwork),
+                                 C.c_int(0))
+        self.lib.oracle_dgeqp4_sketch(C.byref(mi), C.byref(ni), _dptr(A), C.byref(ldi),
+                                      _iptr(jp), _dptr(tau), _dptr(work), C.byref(lw),
+                                      C.byref(info), _dptr(G), 74)
+        return A, jp, tau[:min(m, n)], info.value, work[0]
 
     def dgeqp3(self, A, jpvt=None):
         A = _fortran(A)

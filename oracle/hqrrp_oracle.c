@@ -447,8 +447,11 @@ int oracle_hqrrp(int m, int n, double* A, int lda, int* jpvt, double* tau, int n
 #define SMALL_DGEQPF 250
 #define SMALL_DGEQP3 1000
 
-void oracle_dgeqp4(int* pm, int* pn, double* A, int* plda, int* jpvt, double* tau,
-                   double* work, int* plwork, int* info) {
+/* G_in (optional): the sketch of the HQRRP call on the free block, 74 x
+ * (m - nf) with leading dimension ldg_in, in place of the one the reference
+ * draws there (...var4.c:257-265). */
+static void dgeqp4_impl(int* pm, int* pn, double* A, int* plda, int* jpvt, double* tau,
+                        double* work, int* plwork, int* info, const double* G_in, int ldg_in) {
   const int m = *pm, n = *pn, lda = *plda, mn = imin(m, n);
   const int query = (*plwork == -1);
   int iws = 1;
@@ -516,8 +519,8 @@ void oracle_dgeqp4(int* pm, int* pn, double* A, int* plda, int* jpvt, double* ta
   int* before = malloc(sizeof(int) * (size_t)n);
   if (nf > 0) memcpy(before, jpvt, sizeof(int) * (size_t)n);
   if (nf < mn)
-    *info = oracle_hqrrp(m - nf, n - nf, A + nf + (size_t)nf * lda, lda, jpvt + nf, tau + nf,
-                         64, 10, 1);
+    *info = oracle_hqrrp_sketch(m - nf, n - nf, A + nf + (size_t)nf * lda, lda, jpvt + nf,
+                                tau + nf, 64, 10, 1, G_in, ldg_in);
   if (nf > 0) {
     /* Follow HQRRP's column order in the rows above the factored block. */
     for (int c = nf; c < n; ++c) {
@@ -533,6 +536,16 @@ void oracle_dgeqp4(int* pm, int* pn, double* A, int* plda, int* jpvt, double* ta
   }
   free(before);
   work[0] = iws;
+}
+
+void oracle_dgeqp4(int* pm, int* pn, double* A, int* plda, int* jpvt, double* tau,
+                   double* work, int* plwork, int* info) {
+  dgeqp4_impl(pm, pn, A, plda, jpvt, tau, work, plwork, info, NULL, 0);
+}
+
+void oracle_dgeqp4_sketch(int* pm, int* pn, double* A, int* plda, int* jpvt, double* tau,
+                          double* work, int* plwork, int* info, const double* G, int ldg) {
+  dgeqp4_impl(pm, pn, A, plda, jpvt, tau, work, plwork, info, G, ldg);
 }
 
 /* Plain LAPACK pass-throughs used as the threshold-path oracle. */

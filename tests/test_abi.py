@@ -91,3 +91,21 @@ def test_no_gpu_fails_loudly(hq):
         hq.hqrrp(np.eye(40), 8, 2)
     with pytest.raises(hq.HQRRPError):
         hq.dgeqp4(np.eye(40))
+
+
+@pytest.mark.skipif(HAS_GPU, reason="checks the no-GPU behaviour")
+def test_no_gpu_error_codes(hq):
+    """Host-side failure: without a device, dgeqp4 returns info = 1000 + 1
+    (a CUDA error) with a message, and the HQRRP entry its positive code."""
+    info, _ = _dgeqp4_raw(hq, 40, 30, 40, 200)
+    assert info == 1001
+    assert "device" in hq.last_error()
+    L = hq.load()
+    A = np.eye(40)
+    jp = np.arange(1, 41, dtype=np.int32)
+    tau = np.zeros(40)
+    dp, ip = C.POINTER(C.c_double), C.POINTER(C.c_int)
+    rc = L.NoFLA_HQRRP_WY_blk_var4(40, 40, A.ctypes.data_as(dp), 40, jp.ctypes.data_as(ip),
+                                   tau.ctypes.data_as(dp), 8, 2, 1)
+    assert rc == 1 and hq.last_error()
+    np.testing.assert_array_equal(A, np.eye(40))

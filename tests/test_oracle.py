@@ -64,6 +64,25 @@ def test_oracle_explicit_sketch_equals_drawn_sketch(oracle_lib):
         np.testing.assert_array_equal(x, y)
 
 
+def _nfix(jp, m):
+    return 0 if jp is None else min(m, int(np.count_nonzero(jp)))
+
+
+@pytest.mark.parametrize("m,n,fixed", [(1200, 1100, None), (1100, 1200, 97), (1100, 1050, 9),
+                                       (1030, 1000, 3)])
+def test_oracle_dgeqp4_explicit_sketch_equals_drawn_sketch(oracle_lib, m, n, fixed):
+    """dgeqp4's HQRRP branch fed the reference's own sketch of the free block
+    (74 x (m - nf), srand(12) + polar method) is the drawn-sketch run, bit for
+    bit: the sketch is the only input the explicit form replaces."""
+    A = oracle.gaussian(m, n, m + 3 * n)
+    jp = None if fixed is None else np.array([i % fixed == 0 for i in range(n)], np.int32)
+    G = oracle_lib.sketch(74, m - _nfix(jp, m))
+    a = oracle_lib.dgeqp4(A, jp)
+    b = oracle_lib.dgeqp4_sketch(A, G, jp)
+    for x, y in zip(a[:4], b[:4]):
+        np.testing.assert_array_equal(x, y)
+
+
 @pytest.mark.skipif(not oracle.reference_available(), reason="reference tree not on this host")
 @pytest.mark.parametrize("m,n,nb,pp,ppiv", [(500, 400, 32, 10, 1), (260, 390, 24, 8, 1),
                                             (333, 333, 40, 10, 0), (1000, 1000, 64, 10, 1)])

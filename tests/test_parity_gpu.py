@@ -211,6 +211,12 @@ DGEQP4_CASES = [
     (300, 260, 18, 7),        # dgeqp3 branch with fixed columns
     (999, 999, 22, None),     # last dgeqp3 size
     (120, 90, 23, 4),         # dgeqpf branch with fixed columns
+    # more than 1024 free columns: the column-partitioned wide kernel
+    (300, 2000, 24, None),    # dgeqp3 branch
+    (200, 3000, 25, None),    # dgeqpf branch
+    (999, 5000, 26, None),    # last dgeqp3 size, five times as many columns
+    (400, 1500, 27, 9),       # fixed columns, then 1333 free ones
+    (64, 1025, 28, None),     # one column past the panel kernel's limit
 ]
 
 
@@ -232,3 +238,82 @@ def test_dgeqp4_demo_7x5(hq):
     assert info == 0
     np.testing.assert_array_equal(jp, g["jpvt"])
     assert col_rel_err(Af, g["af"]) <= TOL and gc.rel(tau, g["tau"]) <= TOL
+
+
+# ---- dgeqp4's HQRRP branch (min(m, n) >= 1000) on the reference's sketch ------
+
+def _fixed_marks(n, fixed):
+    return None if fixed is None else np.array([i % fixed == 0 for i in range(n)], np.int32)
+
+
+def _nfix(jp, m):
+    return 0 if jp is None else min(m, int(np.count_nonzero(jp)))
+
+
+DGEQP4_HQRRP_CASES = [
+    # m, n, seed, fixed-column rule (every k-th column fixed) or None
+    (1200, 1100, 41, None),
+    (1100, 1200, 42, 7),      # wide, fixed columns: unpivoted QR + update, then HQRRP
+    (1100, 1050, 43, 9),      # m > n with fixed columns
+    (1000, 1000, 44, None),   # the first size dgeqp4 gives to HQRRP
+    (1500, 1030, 45, 3),      # a third of the columns fixed: HQRRP on 1156 x 686
+]
+
+
+@pytest.mark.parametrize("m,n,seed,fixed", DGEQP4_HQRRP_CASES)
+def test_dgeqp4_hqrrp_branch_matches_oracle(hq, oracle_lib, m, n, seed, fixed):
+    """dgeqp4 (...var4.c:127-300) through the C ABI, its HQRRP(64, 10, 1) call
+    fed the reference's own sketch of the free block: the oracle draws that
+    sketch itself (srand(12) + polar method, as the reference does), the GPU
+    is given the same matrix.  jpvt identical, tau/R/V within 1e-12, and the
+    same LAPACK workspace figure."""
+    A = oracle.gaussian(m, n, seed)
+    jp = _fixed_marks(n, fixed)
+    G = oracle_lib.sketch(74, m - _nfix(jp, m))
+    Ao, jo, to, io, wo = oracle_lib.dgeqp4(A, jp)
+    Ag, jg, tg, ig, wg = hq.dgeqp4(A, jp, G=G)
+    assert ig == io == 0
+    assert_parity((Ag, jg, tg), (Ao, jo, to))
+    assert wg == wo
+
+
+@pytest.mark.parametrize("name", ["dgeqp4_1200x1100", "dgeqp4_1100x1200_fixed"])
+def test_dgeqp4_hqrrp_branch_against_reference_golden(hq, oracle_lib, name):
+    """The GPU dgeqp4 straight against what the reference's dgeqp4 returned
+    (fixtures made by tests/golden/make_golden.py from the compiled reference)."""
+    A, jp, same = gc.case_input(name)
+    if not same:
+        pytest.skip("fixture input not reproducible by this numpy")
+    g = gc.load(name)
+    m, n = A.shape
+    G = oracle_lib.sketch(74, m - _nfix(jp, m))
+    Af, jpv, tau, info, work0 = hq.dgeqp4(A, jp, G=G)
+    assert info == int(g["info"]) and work0 == float(g["work0"])
+    s = gc.summary(Af, jpv, tau, m, n)
+    np.testing.assert_array_equal(s["jpvt"], g["jpvt"])
+    for key in ("tau", "diag", "aw", "atu"):
+        assert gc.rel(s[key], g[key]) <= TOL, key
+
+
+def test_dgeqp4_rows_above_follow_hqrrp_bit_exact(hq, oracle_lib):
+    """The re-pivot of the rows above the free block (...var4.c:267-292) is a
+    pure column permutation.  With unit vectors e_0, e_1, ... as the fixed
+    columns, every fixed-column reflector is the identity (tau = 0), so rows
+    0..nf-1 of the free columns must come out as the input's rows, in HQRRP's
+    column order, bit for bit -- on the GPU and in the oracle alike."""
+    m, n, every = 1100, 1200, 50
+    A = oracle.gaussian(m, n, 46)
+    jp = _fixed_marks(n, every)
+    pos = np.flatnonzero(jp)
+    nf = len(pos)
+    for t, c in enumerate(pos):
+        A[:, c] = 0.0
+        A[t, c] = 1.0
+    G = oracle_lib.sketch(74, m - nf)
+    Ag, jg, tg, ig, _ = hq.dgeqp4(A, jp, G=G)
+    Ao, jo, to, io, _ = oracle_lib.dgeqp4(A, jp)
+    assert ig == io == 0
+    assert np.all(tg[:nf] == 0.0) and np.all(to[:nf] == 0.0)
+    np.testing.assert_array_equal(Ag[:nf, nf:], A[:nf, jg[nf:] - 1])
+    np.testing.assert_array_equal(Ao[:nf, nf:], A[:nf, jo[nf:] - 1])
+    assert_parity((Ag, jg, tg), (Ao, jo, to))

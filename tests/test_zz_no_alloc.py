@@ -72,6 +72,7 @@ def test_noalloc_matches_allocating_entry_two_calls_in_a_row(hq):
         want.append(out)
     bufs = [_buffers(A) for A in inputs]  # every device buffer exists before the calls
     free_before = None
+    pool_before = hq.pool_alloc_count()
     for i, A in enumerate(inputs):
         if i == 1:  # after the one-time set-up done by the first call
             torch.cuda.synchronize()
@@ -81,7 +82,27 @@ def test_noalloc_matches_allocating_entry_two_calls_in_a_row(hq):
         _same(got, want[i])
         assert oracle.quality(A, got[0], got[1], got[2])[0] < 1e-14
     torch.cuda.synchronize()
+    assert hq.pool_alloc_count() == pool_before  # no allocation from the library's pools
     assert torch.cuda.mem_get_info()[0] == free_before  # the second call took no device memory
+
+
+def test_noalloc_tall_matrix_in_place_panel(hq):
+    """20000 x 256: a CTA's rows no longer fit its shared memory, so the
+    kernel works on the matrix in place (global memory) -- the same results
+    as the allocating entry point, again with no pool allocation."""
+    import torch
+    noalloc, alloc = _bind(hq.load())
+    stream = torch.cuda.current_stream().cuda_stream
+    A = oracle.gaussian(20000, 256, 34)
+    rc, *want = _run(alloc, A, _buffers(A), stream)
+    assert rc == 0, hq.last_error()
+    bufs = _buffers(A)
+    pool_before = hq.pool_alloc_count()
+    rc, *got = _run(noalloc, A, bufs, stream)
+    assert rc == 0, hq.last_error()
+    assert hq.pool_alloc_count() == pool_before
+    _same(got, want)
+    assert oracle.quality(A, got[0], got[1], got[2])[0] < 1e-14
 
 
 def test_noalloc_rejects_sizes_beyond_its_limit(hq):
