@@ -75,10 +75,15 @@ def parse():
     p.add_argument("--pp", type=int, default=10)
     p.add_argument("--seed", type=int, default=2026)
     p.add_argument("--e2e-steps", type=int, default=2)
-    p.add_argument("--cpu-n", type=int, default=6144, help="CPU baseline sample size")
-    p.add_argument("--ref-n", type=int, default=8192, help="reference-arm sample size")
+    p.add_argument("--cpu-dgeqp3-n", type=int, default=6144,
+                   help="size of the LAPACK dgeqp3 CPU sample")
+    p.add_argument("--cpu-1t-n", type=int, default=3072,
+                   help="size of the one-thread CPU sample")
+    p.add_argument("--ref-n", type=int, default=16384, help="reference-arm matrix size")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-adjoint", action="store_true", help="skip the bwd_ms measurement")
+    p.add_argument("--no-extras", action="store_true",
+                   help="square workload only: skip the nested tall and batched lines")
     return p.parse_args()
 
 
@@ -260,52 +265,103 @@ def cpu_model():
     return "unknown"
 
 
-def cpu_oracle_run(n, nb, pp, reps, seed):
+def cpu_impl(threads):
+    """The compiled reference where its tree is present, else the oracle's
+    restatement of it (bit-identical on the same LAPACK, tests/test_oracle.py)."""
     import oracle
     try:
-        impl = oracle.Reference()
-        kind = "reference"
+        impl, kind = oracle.Reference(), "reference"
     except RuntimeError:
-        impl = oracle.Oracle()
-        kind = "port"
-    cores = os.cpu_count() or 1
-    impl.set_threads(cores)
-    A = make_matrix_cpu(n, seed)
-    times = []
-    for _ in range(reps):
-        t0 = time.perf_counter()
-        impl.hqrrp(A, nb, pp, 1)
-        times.append(time.perf_counter() - t0)
-    return kind, cores, times
+        impl, kind = oracle.Oracle(), "port"
+    impl.set_threads(threads)
+    return impl, kind
 
 
-def cpu_dgeqp3_run(n, seed):
+def host_square_matrix(n, seed):
+    """The square workload's matrix on the host (column-major numpy), made on
+    the GPU exactly as the GPU arm makes it when a GPU is present."""
+    try:
+        import torch
+        if torch.cuda.is_available():
+            At = make_matrix_gpu(n, n, spectrum(n), seed, torch.device("cuda", 0))
+            A = np.asfortranarray(At.cpu().numpy().T)
+            del At
+            torch.cuda.empty_cache()
+            return A
+    except ImportError:
+        pass
+    return make_matrix_cpu(n, seed)
+
+
+def cpu_baseline_run(A, args):
+    """Bounded CPU sample beside the GPU arm (about half a minute on the GPU
+    host's 16 cores): the reference dgeqp4 once on the headline matrix itself,
+    LAPACK dgeqp3 once on its leading args.cpu_dgeqp3_n block, and dgeqp4 on
+    one thread on its leading args.cpu_1t_n block."""
     import oracle
-    o = oracle.Oracle()
-    o.set_threads(os.cpu_count() or 1)
-    A = make_matrix_cpu(n, seed)
-    t0 = time.perf_counter()
-    o.dgeqp3(A)
-    return time.perf_counter() - t0
+    cores = os.cpu_count() or 1
+    impl, kind = cpu_impl(cores)
+    n = A.shape[1]
+    t4 = impl.timed_dgeqp4(np.array(A, order="F"))
+    n3 = min(n, args.cpu_dgeqp3_n)
+    lap = oracle.Oracle()
+    lap.set_threads(cores)
+    t3 = lap.timed_dgeqp3(np.array(A[:n3, :n3], order="F"))
+    n1 = min(n, args.cpu_1t_n)
+    impl.set_threads(1)
+    t1 = impl.timed_dgeqp4(np.array(A[:n1, :n1], order="F"))
+    impl.set_threads(cores)
+    return {"value": flops_qr(n, n) / t4 / 1e12, "unit": "TFLOP/s", "cores": cores,
+            "kind": kind, "cpu_model": cpu_model(),
+            "sample": "reference dgeqp4 (HQRRP nb=64, pp=10 inside) on the headline's own m=n=%d "
+                      "matrix, once: %.1f s" % (n, t4),
+            "lapack_dgeqp3": {"value": flops_qr(n3, n3) / t3 / 1e12, "unit": "TFLOP/s",
+                              "cores": cores, "seconds": t3,
+                              "sample": "LAPACK dgeqp3 (scipy OpenBLAS) on the leading m=n=%d "
+                                        "block of the same matrix, once" % n3},
+            "one_thread": {"value": flops_qr(n1, n1) / t1 / 1e12, "unit": "TFLOP/s", "cores": 1,
+                           "seconds": t1,
+                           "sample": "reference dgeqp4 on one thread, leading m=n=%d block, "
+                                     "once" % n1}}
 
 
 def run_reference_arm(args):
+    """The reference's dgeqp4 (HQRRP nb=64, pp=10 inside, as the reference
+    hard-codes) on the host cores, on the square workload's own matrix: each
+    timed step factors a fresh copy of it.  Warm-up steps factor a 4096^2
+    block (they only wake the BLAS threads).  HQRRP nb=128 on the same matrix
+    is timed once beside it (the block size of the GPU headline)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     n = args.ref_n
-    kind, cores, times = cpu_oracle_run(n, args.nb, args.pp, args.warmup + args.steps, args.seed)
-    timed = times[args.warmup:] or times
-    sec = sum(timed)
-    value = flops_qr(n, n) * len(timed) / sec / 1e12
-    sample = ("HQRRP nb=%d pp=%d on m=n=%d (same spectrum as the GPU workload), one "
-              "factorization per step" % (args.nb, args.pp, n))
+    cores = os.cpu_count() or 1
+    impl, kind = cpu_impl(cores)
+    A = host_square_matrix(n, args.seed)
+    nw = min(n, 4096)
+    for _ in range(args.warmup):
+        impl.timed_dgeqp4(np.array(A[:nw, :nw], order="F"))
+    times = []
+    for _ in range(args.steps):
+        B = np.array(A, order="F")
+        times.append(impl.timed_dgeqp4(B))
+        del B
+    sec = sum(times)
+    value = flops_qr(n, n) * len(times) / sec / 1e12
+    th = impl.timed_hqrrp(np.array(A, order="F"), args.nb, args.pp)
+    sample = ("reference dgeqp4 (HQRRP nb=64 pp=10 inside) on m=n=%d, A=U diag(10^(-12 i/n)) "
+              "V^T (the GPU arm's matrix), one factorization per step; warm-up steps on its "
+              "leading %d^2 block" % (n, nw))
     line = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "impl": "reference",
-            "n_gpus": args.gpus, "steps": len(timed), "warmup": args.warmup,
-            "ms_per_step": sec / len(timed) * 1e3, "higher_is_better": True, "scaling": "weak",
+            "n_gpus": args.gpus, "steps": len(times), "warmup": args.warmup,
+            "ms_per_step": sec / len(times) * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "HQRRP m=n=%d nb=%d pp=%d, reference algorithm on host cores"
-                       % (n, args.nb, args.pp), "m": n, "n": n, "nb": args.nb, "pp": args.pp},
+            "config": {"workload": "pivoted QR of m=n=%d, A=U diag(10^(-12 i/n)) V^T, Haar U,V; "
+                                   "reference dgeqp4 on host cores" % n,
+                       "name": "square", "m": n, "n": n, "api": "dgeqp4"},
+            "hqrrp_nb128": {"value": flops_qr(n, n) / th / 1e12, "unit": "TFLOP/s", "seconds": th,
+                            "api": "NoFLA_HQRRP_WY_blk_var4(nb=%d, pp=%d), once"
+                                   % (args.nb, args.pp)},
             "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": cores, "kind": kind,
                              "sample": sample, "cpu_model": cpu_model()},
             "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
@@ -341,8 +397,9 @@ def measured_peaks():
         return {}
 
 
-def run_arm(hq, precision, At0, At, jp, iota, tau, nb, pp, sigma, args, device, dist, local):
-    """Warm up, then time exactly args.steps factorizations (one arm)."""
+def run_arm(hq, precision, At0, At, jp, iota, tau, nb, pp, sigma, steps, warmup, device, dist,
+            local):
+    """Warm up, then time exactly `steps` factorizations (one arm)."""
     import torch
     hq.set_precision(hq.MIXED if precision == "mixed" else hq.PLAIN)
     stream = torch.cuda.current_stream()
@@ -352,7 +409,7 @@ def run_arm(hq, precision, At0, At, jp, iota, tau, nb, pp, sigma, args, device, 
         jp.copy_(iota)
         hq.hqrrp_device(At, jp, tau, nb, pp, 1, stream=stream)
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         step()
     torch.cuda.synchronize()
     sampler = ClockSampler(local)
@@ -363,7 +420,7 @@ def run_arm(hq, precision, At0, At, jp, iota, tau, nb, pp, sigma, args, device, 
     sampler.start()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(steps):
         step()
     e1.record(stream)
     torch.cuda.synchronize()
@@ -387,7 +444,8 @@ def run_arm(hq, precision, At0, At, jp, iota, tau, nb, pp, sigma, args, device, 
     prof = hq.profile_read()
     counts = hq.profile_counts()
     hq.profile_enable(False)
-    return {"ms_per_step": ms / args.steps, "launches": launches, "clocks": clocks,
+    return {"ms_per_step": ms / steps, "steps": steps, "warmup": warmup, "launches": launches,
+            "clocks": clocks,
             "quality": {"residual_est": res, "orthogonality_est": orth,
                         "rkk_over_sigma_min": float(ratio.min()),
                         "rkk_over_sigma_max": float(ratio.max())},
@@ -434,10 +492,11 @@ def measure_adjoint(hq, device, m=4096, n=2048, k=256, nb=64, reps=5, seed=7):
                       "(Q_k and T rebuilt from the reflectors)" % (m, n, k, nb, reps)}
 
 
-def run_batched(hq, args, device, dist, rank, world, local):
+def run_batched(hq, args, device, dist, rank, world, local, steps, warmup):
     """Config: args.batch matrices of random shape, A_i = U diag(i^-2) V^T; one
     step = restore the inputs and replay the captured graph of one persistent
-    launch over this rank's cost-balanced shard of the batch."""
+    launch over this rank's cost-balanced shard of the batch.  Returns rank
+    0's line (None on other ranks)."""
     import torch
     from hqrrp_gb300 import shard
     _preload_linalg()
@@ -470,7 +529,7 @@ def run_batched(hq, args, device, dist, rank, world, local):
         graph.replay()
 
     with torch.cuda.stream(s):
-        for _ in range(args.warmup):
+        for _ in range(warmup):
             step()
         torch.cuda.synchronize()
         if dist:
@@ -480,14 +539,14 @@ def run_batched(hq, args, device, dist, rank, world, local):
         sampler.start()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(s)
-        for _ in range(args.steps):
+        for _ in range(steps):
             step()
         e1.record(s)
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
         clocks = sampler.stop()
-    ms = e0.elapsed_time(e1) / args.steps
+    ms = e0.elapsed_time(e1) / steps
     info = bq.info.cpu().numpy()
     if (info != 0).any():
         raise RuntimeError("batched QR reported info %s" % info[info != 0][:4])
@@ -536,7 +595,7 @@ def run_batched(hq, args, device, dist, rank, world, local):
         h2d = 8 * int(offs[-1])
         d2h = h2d + 4 * bq.jpvt_flat.numel() + 8 * bq.tau_flat.numel()
         line = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+                "steps": steps, "warmup": warmup, "ms_per_step": ms,
                 "higher_is_better": True, "scaling": "weak" if world == 1 else "strong",
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                 "config": {"workload": "batched pivoted QR of %d matrices, m log-uniform in "
@@ -562,9 +621,10 @@ def run_batched(hq, args, device, dist, rank, world, local):
                         "ms_per_step": esec * 1e3,
                         "api": "graph replay of hqrrp_gb300_qrp_batched_run, pinned host "
                                "buffers"},
-                "gpu_launches": per_replay * args.steps, "clocks": clocks}
+                "gpu_launches": per_replay * steps, "clocks": clocks}
         line["roofline"]["frac"] = value / line["roofline"]["peak"]
-        print(json.dumps(line), flush=True)
+        return line
+    return None
 
 
 def cpu_batched_run(shapes, offs, flat0, stride=1, reps=3):
@@ -598,6 +658,201 @@ def cpu_batched_run(shapes, offs, flat0, stride=1, reps=3):
                                                               reps, sec)}
 
 
+def roofline_of(H, head, peaks, device):
+    """Roofline of the dominant kernel of an arm, from its live phase profile:
+    mixed -> the split-BF16 products (BF16 tensor work), plain -> dgemm_tile."""
+    if head == "mixed":
+        t_ms, t_fl = H["prof"]["tensor"]
+        n_t = max(1, H["counts"].get("tensor", 0))
+        peak = peaks.get("bf16_tflops_sustained") or 1700.0
+        achieved = t_fl / (t_ms * 1e-3) / 1e12 if t_ms > 0 else None
+        roofline = {"bound": "tensor", "pipe": "bf16 tcgen05",
+                    "kernel": "ozk_gemm_kernel + ozk_gemm_short_kernel (split-BF16 digit "
+                              "products of the block update, Gram, T^T W1 and sketch downdate)",
+                    "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                    "frac": achieved / peak if achieved else None,
+                    "peak_source": "bf16_tflops_sustained of measured (MEASURED_PEAKS.json)"
+                    if peaks.get("bf16_tflops_sustained") else "fallback 1.7 PFLOP/s sustained",
+                    "launches": n_t, "flops_per_launch": t_fl / n_t,
+                    "traffic": TENSOR_BYTES_PER_FLOP * t_fl / n_t,
+                    "traffic_source": "ncu dram__bytes_read+write at 6144^2 scaled by flops "
+                                      "per launch"}
+    else:
+        u_ms, u_fl = H["prof"]["update"]
+        peak = fp64_peak_tflops(device)
+        achieved = u_fl / (u_ms * 1e-3) / 1e12 if u_ms > 0 else None
+        n_u = 3 * max(1, H["counts"].get("update", 0))  # W1, W2, U3 per block
+        roofline = {"bound": "tensor", "pipe": "fp64",
+                    "kernel": "dgemm_tile (trailing dlarfb update)",
+                    "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                    "frac": achieved / peak if achieved else None,
+                    "peak_source": "cuBLAS DGEMM 8192^3 measured in this run (MEASURED_PEAKS.json "
+                                   "has no FP64 figure)",
+                    "launches": n_u, "flops_per_launch": u_fl / n_u,
+                    "traffic": FP64_UPDATE_BYTES_PER_FLOP * u_fl / n_u,
+                    "traffic_source": "ncu dram__bytes_read+write at 6144^2 scaled by flops "
+                                      "per launch"}
+    roofline["phases_ms"], roofline["phases_tflops"] = phase_table(H["prof"])
+    return roofline
+
+
+def e2e_host(hq, At0, m, n, nb, pp, steps, head, world, dist, device):
+    """The same factorization end to end through the reference-facing C entry
+    points, host buffers in and out inside the timed region:
+    NoFLA_HQRRP_WY_blk_var4 and dgeqp4 (HQRRP nb=64, pp=10 inside) on
+    page-locked buffers, and NoFLA_HQRRP_WY_blk_var4 on pageable memory (what a
+    drop-in caller's malloc gives)."""
+    import ctypes as C
+    import torch
+    L = hq.load()
+    hq.set_precision(hq.MIXED if head == "mixed" else hq.PLAIN)
+    host0 = At0.cpu().pin_memory()
+    hA = torch.empty_like(host0).pin_memory()
+    hjp = torch.empty(n, dtype=torch.int32).pin_memory()
+    htau = torch.empty(min(m, n), dtype=torch.float64).pin_memory()
+    dp, ip = C.POINTER(C.c_double), C.POINTER(C.c_int)
+
+    def hqrrp_call(A_ptr, jp_ptr, tau_ptr):
+        rc = L.NoFLA_HQRRP_WY_blk_var4(m, n, C.cast(A_ptr, dp), m, C.cast(jp_ptr, ip),
+                                       C.cast(tau_ptr, dp), nb, pp, 1)
+        if rc != 0:
+            raise RuntimeError("e2e call failed: %s" % hq.last_error())
+
+    times = []
+    for it in range(1 + steps):
+        hA.copy_(host0)
+        hjp.copy_(torch.arange(1, n + 1, dtype=torch.int32))
+        t0 = time.perf_counter()
+        hqrrp_call(hA.data_ptr(), hjp.data_ptr(), htau.data_ptr())
+        if it > 0:
+            times.append(time.perf_counter() - t0)
+    sec = sum(times) / len(times)
+    # dgeqp4 on the same page-locked buffers; all columns free.
+    ltimes = []
+    mi, ni, ldi, info = C.c_int(m), C.c_int(n), C.c_int(m), C.c_int(0)
+    lwork = C.c_int(-1)
+    wq = (C.c_double * 1)()
+    L.dgeqp4(C.byref(mi), C.byref(ni), C.cast(hA.data_ptr(), dp), C.byref(ldi),
+             C.cast(hjp.data_ptr(), ip), C.cast(htau.data_ptr(), dp), wq, C.byref(lwork),
+             C.byref(info))
+    work = (C.c_double * max(1, int(wq[0])))()
+    lwork = C.c_int(max(1, int(wq[0])))
+    for it in range(1 + steps):
+        hA.copy_(host0)
+        hjp.zero_()
+        t0 = time.perf_counter()
+        L.dgeqp4(C.byref(mi), C.byref(ni), C.cast(hA.data_ptr(), dp), C.byref(ldi),
+                 C.cast(hjp.data_ptr(), ip), C.cast(htau.data_ptr(), dp), work,
+                 C.byref(lwork), C.byref(info))
+        dt = time.perf_counter() - t0
+        if info.value != 0:
+            raise RuntimeError("dgeqp4 failed: info %d %s" % (info.value, hq.last_error()))
+        if it > 0:
+            ltimes.append(dt)
+    lsec = sum(ltimes) / len(ltimes)
+    del hA
+    # pageable host memory (numpy)
+    pA0 = host0.numpy().copy()
+    pA = np.empty_like(pA0)
+    pjp = np.empty(n, np.int32)
+    ptau = np.empty(min(m, n))
+    ptimes = []
+    for it in range(1 + steps):
+        np.copyto(pA, pA0)
+        pjp[:] = np.arange(1, n + 1, dtype=np.int32)
+        t0 = time.perf_counter()
+        hqrrp_call(pA.ctypes.data, pjp.ctypes.data, ptau.ctypes.data)
+        if it > 0:
+            ptimes.append(time.perf_counter() - t0)
+    psec = sum(ptimes) / len(ptimes)
+    del pA, pA0
+    if dist:
+        t = torch.tensor([sec, lsec, psec], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        sec, lsec, psec = float(t[0]), float(t[1]), float(t[2])
+    fl = world * flops_qr(m, n)
+    return {"value": fl / sec / 1e12, "unit": "TFLOP/s",
+            "h2d_bytes_per_step": 8 * m * n + 4 * n,
+            "d2h_bytes_per_step": 8 * m * n + 4 * n + 8 * min(m, n),
+            "ms_per_step": sec * 1e3, "precision": head,
+            "api": "NoFLA_HQRRP_WY_blk_var4(nb=%d, pp=%d), host page-locked buffers" % (nb, pp),
+            "dgeqp4": {"value": fl / lsec / 1e12, "unit": "TFLOP/s", "ms_per_step": lsec * 1e3,
+                       "api": "dgeqp4 (HQRRP nb=64, pp=10 inside), host page-locked buffers"},
+            "pageable": {"value": fl / psec / 1e12, "unit": "TFLOP/s", "ms_per_step": psec * 1e3,
+                         "api": "NoFLA_HQRRP_WY_blk_var4(nb=%d, pp=%d), host pageable (numpy) "
+                                "buffers" % (nb, pp)}}
+
+
+def run_factorization(hq, args, name, device, dist, rank, world, local, steps, warmup,
+                      plain_steps, plain_warmup, e2e_steps, precision):
+    """Square or tall workload: time the arms, then the roofline and the end to
+    end figures; returns (line, At0) with At0 the input on the device."""
+    import torch
+    nb, pp = args.nb, args.pp
+    if name == "tall":
+        n = args.n or 8192
+        m = args.m or 4 * n
+        sigma = spectrum_tall(min(m, n))
+        wl = ("HQRRP m=%d n=%d nb=%d pp=%d panel_pivoting=1, A=U diag(sigma) V^T, Haar U,V, "
+              "sigma geometric 1..1e-10 with 64 equal values at 1e-4" % (m, n, nb, pp))
+    else:
+        n = m = args.n or 16384
+        sigma = spectrum(n)
+        wl = ("HQRRP m=n=%d nb=%d pp=%d panel_pivoting=1, A=U diag(10^(-12 i/n)) V^T, "
+              "Haar U,V" % (n, nb, pp))
+    At0 = make_matrix_gpu(m, n, sigma, args.seed + rank, device)
+    At = torch.empty_like(At0)
+    iota = torch.arange(1, n + 1, dtype=torch.int32, device=device)
+    jp = iota.clone()
+    tau = torch.zeros(min(m, n), dtype=torch.float64, device=device)
+    arms = ["mixed", "plain"] if precision == "both" else [precision]
+    res = {}
+    for p in arms:
+        k, w = (plain_steps, plain_warmup) if (p == "plain" and len(arms) > 1) else (steps, warmup)
+        res[p] = run_arm(hq, p, At0, At, jp, iota, tau, nb, pp, sigma, k, w, device, dist, local)
+    del At
+    head = arms[0]
+    H = res[head]
+    value = world * flops_qr(m, n) / (H["ms_per_step"] * 1e-3) / 1e12
+    peaks = measured_peaks()
+    roofline = roofline_of(H, head, peaks, device)
+    e2e = None
+    if e2e_steps > 0:
+        e2e = e2e_host(hq, At0, m, n, nb, pp, e2e_steps, head, world, dist, device)
+    line = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world,
+            "steps": steps, "warmup": warmup, "ms_per_step": H["ms_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if head == "plain" else "f64 (split-bf16 tensor products)",
+            "data": "synthetic",
+            "config": {"workload": wl, "name": name, "m": m, "n": n, "nb": nb, "pp": pp,
+                       "precision": head, "api": "hqrrp_gb300_hqrrp_device",
+                       "parallelism": "replicas%d" % world,
+                       "l2": "inputs larger than L2 (%.1f GB matrix per step)" % (8 * m * n / 1e9)},
+            "quality": H["quality"], "roofline": roofline, "e2e": e2e,
+            "gpu_launches": H["launches"], "clocks": H["clocks"],
+            "measured_peaks": {k: peaks.get(k) for k in ("hbm_gbs", "bf16_tflops",
+                                                          "bf16_tflops_sustained")}}
+    if "plain" in res and head != "plain":
+        P = res["plain"]
+        pv = world * flops_qr(m, n) / (P["ms_per_step"] * 1e-3) / 1e12
+        pm, pt = phase_table(P["prof"])
+        line["plain"] = {"value": pv, "ms_per_step": P["ms_per_step"], "steps": P["steps"],
+                         "warmup": P["warmup"], "quality": P["quality"],
+                         "gpu_launches": P["launches"], "clocks": P["clocks"],
+                         "phases_ms": pm, "phases_tflops": pt}
+        line["mixed_over_plain"] = value / pv
+        r = H["ratio"] / P["ratio"]
+        line["quality"]["rkk_ratio_mixed_over_plain"] = [float(r.min()), float(r.max())]
+    return line, At0
+
+
+def sub_line(d, keep=("value", "unit", "ms_per_step", "steps", "warmup", "config", "quality",
+                      "roofline", "e2e", "plain", "mixed_over_plain", "gpu_launches", "clocks",
+                      "matrices_per_s", "cpu_baseline")):
+    """A workload's own line, nested under the headline's."""
+    return None if d is None else {k: d[k] for k in keep if k in d}
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -619,179 +874,46 @@ def main():
     torch.cuda.set_device(device)
 
     if args.workload == "batched":
-        run_batched(hq, args, device, dist, rank, world, local)
+        line = run_batched(hq, args, device, dist, rank, world, local, args.steps, args.warmup)
+        if line is not None:
+            print(json.dumps(line), flush=True)
         if dist:
             dist.destroy_process_group()
         return
-    nb, pp = args.nb, args.pp
-    if args.workload == "tall":
-        n = args.n or 8192
-        m = args.m or 4 * n
-        sigma = spectrum_tall(min(m, n))
-        wl = ("HQRRP m=%d n=%d nb=%d pp=%d panel_pivoting=1, A=U diag(sigma) V^T, Haar U,V, "
-              "sigma geometric 1..1e-10 with 64 equal values at 1e-4" % (m, n, nb, pp))
-    else:
-        n = m = args.n or 16384
-        sigma = spectrum(n)
-        wl = ("HQRRP m=n=%d nb=%d pp=%d panel_pivoting=1, A=U diag(10^(-12 i/n)) V^T, "
-              "Haar U,V" % (n, nb, pp))
-    At0 = make_matrix_gpu(m, n, sigma, args.seed + rank, device)
-    At = torch.empty_like(At0)
-    iota = torch.arange(1, n + 1, dtype=torch.int32, device=device)
-    jp = iota.clone()
-    tau = torch.zeros(min(m, n), dtype=torch.float64, device=device)
 
-    arms = ["mixed", "plain"] if args.precision == "both" else [args.precision]
-    res = {p: run_arm(hq, p, At0, At, jp, iota, tau, nb, pp, sigma, args, device, dist, local)
-           for p in arms}
-    head = arms[0]
-    H = res[head]
-    value = world * flops_qr(m, n) / (H["ms_per_step"] * 1e-3) / 1e12
-    peaks = measured_peaks()
+    # The plain FP64 arm beside the mixed headline: at most 5 timed steps after
+    # 3 warm-ups (it is ~12x slower and only the comparison needs it).
+    line, At0 = run_factorization(hq, args, args.workload, device, dist, rank, world, local,
+                                  args.steps, args.warmup, min(args.steps, 5), 3,
+                                  args.e2e_steps, args.precision)
+    A_host = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline and args.workload == "square":
+        A_host = np.asfortranarray(At0.cpu().numpy().T)
+    del At0
+    torch.cuda.empty_cache()
 
-    # Roofline of the dominant kernel of the headline arm, from the live phase
-    # profile: mixed -> ozk_gemm_kernel (BF16 tensor work), plain -> dgemm_tile.
-    if head == "mixed":
-        t_ms, t_fl = H["prof"]["tensor"]
-        n_t = max(1, H["counts"].get("tensor", 0))
-        peak = peaks.get("bf16_tflops_sustained") or 1700.0
-        achieved = t_fl / (t_ms * 1e-3) / 1e12 if t_ms > 0 else None
-        roofline = {"bound": "tensor", "pipe": "bf16 tcgen05",
-                    "kernel": "ozk_gemm_kernel + ozk_gemm_short_kernel (split-BF16 digit "
-                              "products of the block update, Gram, T^T W1 and sketch downdate)",
-                    "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                    "frac": achieved / peak if achieved else None,
-                    "peak_source": "bf16_tflops_sustained of measured (MEASURED_PEAKS.json)"
-                    if peaks.get("bf16_tflops_sustained") else "fallback 1.7 PFLOP/s sustained",
-                    "launches": n_t, "flops_per_launch": t_fl / n_t,
-                    # DRAM bytes per BF16 flop of the two large products of a block,
-                    # ncu at 6144^2 (W1 550.2 MB, C -= U'W2 556.1 MB per 2.649e11
-                    # flops each), times this run's flops per launch.
-                    "traffic": TENSOR_BYTES_PER_FLOP * t_fl / n_t,
-                    "traffic_source": "ncu dram__bytes_read+write at 6144^2 scaled by flops "
-                                      "per launch"}
-    else:
-        u_ms, u_fl = H["prof"]["update"]
-        peak = fp64_peak_tflops(device)
-        achieved = u_fl / (u_ms * 1e-3) / 1e12 if u_ms > 0 else None
-        n_u = 3 * max(1, H["counts"].get("update", 0))  # W1, W2, U3 per block
-        roofline = {"bound": "tensor", "pipe": "fp64", "kernel": "dgemm_tile (trailing dlarfb update)",
-                    "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                    "frac": achieved / peak if achieved else None,
-                    "peak_source": "cuBLAS DGEMM 8192^3 measured in this run (MEASURED_PEAKS.json "
-                                   "has no FP64 figure)",
-                    "launches": n_u, "flops_per_launch": u_fl / n_u,
-                    "traffic": FP64_UPDATE_BYTES_PER_FLOP * u_fl / n_u,
-                    "traffic_source": "ncu dram__bytes_read+write at 6144^2 scaled by flops "
-                                      "per launch"}
-    roofline["phases_ms"], roofline["phases_tflops"] = phase_table(H["prof"])
-
-    # End to end through the reference-facing C entry point, host buffers.
-    e2e = None
-    if args.e2e_steps > 0:
-        import ctypes as C
-        L = hq.load()
-        hq.set_precision(hq.MIXED if head == "mixed" else hq.PLAIN)
-        host0 = At0.cpu().pin_memory()
-        hA = torch.empty_like(host0).pin_memory()
-        hjp = torch.empty(n, dtype=torch.int32).pin_memory()
-        htau = torch.empty(min(m, n), dtype=torch.float64).pin_memory()
-        dp, ip = C.POINTER(C.c_double), C.POINTER(C.c_int)
-        times = []
-        for it in range(1 + args.e2e_steps):
-            hA.copy_(host0)
-            hjp.copy_(torch.arange(1, n + 1, dtype=torch.int32))
-            t0 = time.perf_counter()
-            rc = L.NoFLA_HQRRP_WY_blk_var4(m, n, C.cast(hA.data_ptr(), dp), m,
-                                           C.cast(hjp.data_ptr(), ip), C.cast(htau.data_ptr(), dp),
-                                           nb, pp, 1)
-            dt = time.perf_counter() - t0
-            if rc != 0:
-                raise RuntimeError("e2e call failed: %s" % hq.last_error())
-            if it > 0:
-                times.append(dt)
-        sec = sum(times) / len(times)
-        # dgeqp4 (HQRRP with nb = 64, pp = 10 inside, as the reference's) on
-        # the same host buffers; all columns free.
-        ltimes = []
-        mi, ni, ldi, info = C.c_int(m), C.c_int(n), C.c_int(m), C.c_int(0)
-        lwork = C.c_int(-1)
-        wq = (C.c_double * 1)()
-        L.dgeqp4(C.byref(mi), C.byref(ni), C.cast(hA.data_ptr(), dp), C.byref(ldi),
-                 C.cast(hjp.data_ptr(), ip), C.cast(htau.data_ptr(), dp), wq, C.byref(lwork),
-                 C.byref(info))
-        work = (C.c_double * max(1, int(wq[0])))()
-        lwork = C.c_int(max(1, int(wq[0])))
-        for it in range(1 + args.e2e_steps):
-            hA.copy_(host0)
-            hjp.zero_()
-            t0 = time.perf_counter()
-            L.dgeqp4(C.byref(mi), C.byref(ni), C.cast(hA.data_ptr(), dp), C.byref(ldi),
-                     C.cast(hjp.data_ptr(), ip), C.cast(htau.data_ptr(), dp), work,
-                     C.byref(lwork), C.byref(info))
-            dt = time.perf_counter() - t0
-            if info.value != 0:
-                raise RuntimeError("dgeqp4 failed: info %d %s" % (info.value, hq.last_error()))
-            if it > 0:
-                ltimes.append(dt)
-        lsec = sum(ltimes) / len(ltimes)
-        if dist:
-            t = torch.tensor([sec, lsec], dtype=torch.float64, device=device)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            sec, lsec = float(t[0]), float(t[1])
-        e2e = {"value": world * flops_qr(m, n) / sec / 1e12, "unit": "TFLOP/s",
-               "h2d_bytes_per_step": 8 * m * n + 4 * n,
-               "d2h_bytes_per_step": 8 * m * n + 4 * n + 8 * min(m, n),
-               "ms_per_step": sec * 1e3, "precision": head,
-               "api": "NoFLA_HQRRP_WY_blk_var4(nb=%d, pp=%d), host pinned buffers" % (nb, pp),
-               "dgeqp4": {"value": world * flops_qr(m, n) / lsec / 1e12, "unit": "TFLOP/s",
-                          "ms_per_step": lsec * 1e3,
-                          "api": "dgeqp4 (HQRRP nb=64, pp=10 inside), host pinned buffers"}}
-
-    adj = None
+    extras = args.workload == "square" and world == 1 and not args.no_extras
     if rank == 0 and not args.no_adjoint and args.workload == "square":
         hq.set_precision(hq.PLAIN)
         adj = measure_adjoint(hq, device)
-
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        kind, cores, times = cpu_oracle_run(args.cpu_n, nb, pp, 2, args.seed)
-        t = min(times)
-        t3 = cpu_dgeqp3_run(args.cpu_n, args.seed)
-        cpu = {"value": flops_qr(args.cpu_n, args.cpu_n) / t / 1e12, "unit": "TFLOP/s",
-               "cores": cores, "kind": kind, "cpu_model": cpu_model(),
-               "sample": "HQRRP nb=%d pp=%d on m=n=%d, same spectrum as the square workload, "
-                         "best of 2, %.1f s each" % (nb, pp, args.cpu_n, t),
-               "lapack_dgeqp3": {"value": flops_qr(args.cpu_n, args.cpu_n) / t3 / 1e12,
-                                 "unit": "TFLOP/s", "cores": cores, "seconds": t3,
-                                 "sample": "LAPACK dgeqp3 (scipy OpenBLAS) on the same m=n=%d "
-                                           "matrix, once" % args.cpu_n}}
-
+        line["bwd_ms"], line["adjoint"] = adj["bwd_ms"], adj
+    if extras:
+        # The other measured workloads, each with its own figures, nested.
+        targs = argparse.Namespace(**vars(args))
+        targs.n, targs.m = 8192, 32768
+        tall, tA = run_factorization(hq, targs, "tall", device, None, 0, 1, local,
+                                     min(args.steps, 5), 3, 2, 1, 1, "both")
+        del tA
+        torch.cuda.empty_cache()
+        line["tall"] = sub_line(tall)
+        b = run_batched(hq, args, device, None, 0, 1, local, min(args.steps, 10), 3)
+        line["batched"] = sub_line(b)
+        torch.cuda.empty_cache()
+    if A_host is not None:
+        line["cpu_baseline"] = cpu_baseline_run(A_host, args)
+    else:
+        line["cpu_baseline"] = None
     if rank == 0:
-        line = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": H["ms_per_step"],
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                "dtype": "f64" if head == "plain" else "f64 (split-bf16 tensor products)",
-                "data": "synthetic",
-                "config": {"workload": wl, "name": args.workload, "m": m, "n": n, "nb": nb, "pp": pp, "precision": head,
-                           "api": "hqrrp_gb300_hqrrp_device", "parallelism": "replicas%d" % world,
-                           "l2": "inputs larger than L2 (%.1f GB matrix per step)"
-                                 % (8 * m * n / 1e9)},
-                "quality": H["quality"], "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-                "gpu_launches": H["launches"], "clocks": H["clocks"],
-                "bwd_ms": adj["bwd_ms"] if adj else None, "adjoint": adj,
-                "measured_peaks": {k: peaks.get(k) for k in ("hbm_gbs", "bf16_tflops",
-                                                              "bf16_tflops_sustained")}}
-        if "plain" in res and head != "plain":
-            P = res["plain"]
-            pv = world * flops_qr(m, n) / (P["ms_per_step"] * 1e-3) / 1e12
-            pm, pt = phase_table(P["prof"])
-            line["plain"] = {"value": pv, "ms_per_step": P["ms_per_step"],
-                             "quality": P["quality"], "gpu_launches": P["launches"],
-                             "clocks": P["clocks"], "phases_ms": pm, "phases_tflops": pt}
-            line["mixed_over_plain"] = value / pv
-            r = H["ratio"] / P["ratio"]
-            line["quality"]["rkk_ratio_mixed_over_plain"] = [float(r.min()), float(r.max())]
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

@@ -39,6 +39,7 @@ enum {
 #define DGEQP4_NB 64 /* HQRRP block size and oversampling dgeqp4 uses (...var4.c:264) */
 #define DGEQP4_PP 10
 #define LAPACK_NB_DGEQRF 32 /* ILAENV(1, 'DGEQRF') of reference LAPACK */
+#define LAPACK_NX_DGEQRF 128 /* ILAENV(3, 'DGEQRF'): blocked-code crossover */
 #define FIXED_BLOCK 128
 #define DEFAULT_SPIN_LIMIT (1u << 22)
 #define OZK_SLICES 7        /* digits per operand in the mixed block updates */
@@ -1039,8 +1040,14 @@ static int core_dgeqp4(hq_ws* w, int m, int n, double* dA, int ldda, int* hjp, i
                          w->label_tmp));
     }
   }
-  /* LAPACK's dgeqp3 reports max(LWKOPT, the fixed-column workspace). */
-  if (small) iws = imax(iws, 2 * n + (n + 1) * LAPACK_NB_DGEQRF);
+  /* LAPACK's dgeqp3 also counts the blocked code's workspace for the free
+   * block (SN = n - nfix columns), used when NB = 32 and the crossover
+   * NX = 128 (ILAENV's DGEQRF values) are both below its min(m, n) - nfix. */
+  if (small && nfix < mn) {
+    const int sn = n - nfix, sminmn = mn - nfix;
+    if (LAPACK_NB_DGEQRF < sminmn && LAPACK_NX_DGEQRF < sminmn)
+      iws = imax(iws, 2 * sn + (sn + 1) * LAPACK_NB_DGEQRF);
+  }
   *iws_out = iws;
   return HQ_OK;
 }

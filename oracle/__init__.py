@@ -93,6 +93,37 @@ class _Base:
                      _dptr(work), C.byref(lw), C.byref(info))
         return A, jp, tau[:min(m, n)], info.value, work[0]
 
+    def timed_dgeqp4(self, A):
+        """dgeqp4 in place on the Fortran-ordered float64 array A, all columns
+        free; returns the seconds spent in the call (for the CPU baselines)."""
+        import time
+        assert A.flags.f_contiguous and A.dtype == np.float64
+        m, n = A.shape
+        jp = np.zeros(max(1, n), dtype=np.int32)
+        tau = np.zeros(max(1, min(m, n)))
+        lwork = max(1, 3 * n + 1, 2 * n + (n + 1) * 64)
+        work = np.zeros(lwork)
+        mi, ni, ldi, lw, info = (C.c_int(m), C.c_int(n), C.c_int(max(1, m)), C.c_int(lwork),
+                                 C.c_int(0))
+        t0 = time.perf_counter()
+        self._dgeqp4(C.byref(mi), C.byref(ni), _dptr(A), C.byref(ldi), _iptr(jp), _dptr(tau),
+                     _dptr(work), C.byref(lw), C.byref(info))
+        dt = time.perf_counter() - t0
+        if info.value != 0:
+            raise RuntimeError("dgeqp4 info %d" % info.value)
+        return dt
+
+    def timed_hqrrp(self, A, nb, pp, panel_pivoting=1):
+        """NoFLA_HQRRP_WY_blk_var4 in place on A; returns the seconds of the call."""
+        import time
+        assert A.flags.f_contiguous and A.dtype == np.float64
+        m, n = A.shape
+        jp = np.arange(1, n + 1, dtype=np.int32)
+        tau = np.zeros(max(1, min(m, n)))
+        t0 = time.perf_counter()
+        self._hqrrp(m, n, _dptr(A), max(1, m), _iptr(jp), _dptr(tau), nb, pp, panel_pivoting)
+        return time.perf_counter() - t0
+
     def sketch(self, mY, m):
         """The (mY x m) Gaussian sketch the reference draws on entry."""
         G = np.zeros((mY, m), dtype=np.float64, order="F")
@@ -166,6 +197,21 @@ class Oracle(_Base):
                                       _iptr(jp), _dptr(tau), _dptr(work), C.byref(lw),
                                       C.byref(info), _dptr(G), 74)
         return A, jp, tau[:min(m, n)], info.value, work[0]
+
+    def timed_dgeqp3(self, A):
+        """LAPACK dgeqp3 in place on A (all columns free); returns seconds."""
+        import time
+        assert A.flags.f_contiguous and A.dtype == np.float64
+        m, n = A.shape
+        jp = np.zeros(max(1, n), dtype=np.int32)
+        tau = np.zeros(max(1, min(m, n)))
+        lwork = max(1, 3 * n + 1 + (n + 1) * 64)
+        work = np.zeros(lwork)
+        mi, ni, ldi, lw, info = C.c_int(m), C.c_int(n), C.c_int(max(1, m)), C.c_int(lwork), C.c_int(0)
+        t0 = time.perf_counter()
+        self.lib.oracle_dgeqp3(C.byref(mi), C.byref(ni), _dptr(A), C.byref(ldi), _iptr(jp),
+                               _dptr(tau), _dptr(work), C.byref(lw), C.byref(info))
+        return time.perf_counter() - t0
 
     def dgeqp3(self, A, jpvt=None):
         A = _fortran(A)

@@ -13,8 +13,12 @@
 * Adjoint: the truncated rank-256 factorization of a 4096 x 2048 matrix with
   sigma_i = i^-2: the gradient of L = <W, Q_k R_k P^T> (pivots fixed) against
   torch's FP64 autograd of an unpivoted QR of A P (relative 1e-10 normwise)
-  and against a central difference (h = 1e-6) of that fixed-pivot loss
-  (relative 1e-6).
+  and against a central difference (h = 1e-6) of that fixed-pivot loss.  The
+  difference quotient itself carries a rounding error of about
+  kappa(R_11) * eps * |L| / h: the loss goes through a QR of A P's first 256
+  columns, whose condition is sigma_1 / sigma_256 ~ 6.5e4, so |L| ~ 1 is known
+  to ~1e-11 and the quotient to ~1e-5.  Its bar is therefore 3e-4 relative
+  (the small cases in test_adjoint_gpu.py keep 1e-6).
 """
 import numpy as np
 import pytest
@@ -117,7 +121,8 @@ def test_adjoint_workload_full_size(hq):
     assert float(torch.linalg.norm(G - ref) / torch.linalg.norm(ref)) <= 1e-10
     # the forward of the library is that loss at A (pivots of the same run)
     Ahat = hq.lowrank(Ft, jp, tau, k, nb).T
-    assert abs(float((W * Ahat).sum()) - float(L)) <= 1e-10 * abs(float(L))
+    Lv = float(L.detach())
+    assert abs(float((W * Ahat).sum()) - Lv) <= 1e-10 * abs(Lv)
     # central difference of the fixed-pivot loss in one random direction
     E = torch.randn(m, n, dtype=torch.float64, device=dev, generator=g)
     E /= torch.linalg.norm(E)
@@ -125,4 +130,4 @@ def test_adjoint_workload_full_size(hq):
     with torch.no_grad():
         fd = (float(loss(At.T + h * E)) - float(loss(At.T - h * E))) / (2 * h)
     an = float((G * E).sum())
-    assert abs(fd - an) <= 1e-6 * max(abs(an), float(torch.linalg.norm(G)) * 1e-3), (fd, an)
+    assert abs(fd - an) <= 3e-4 * abs(an), (fd, an)
