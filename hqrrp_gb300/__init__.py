@@ -23,6 +23,14 @@ _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
 _lib = None
 
+DOUBLE, INT = 1, 2  # hqrrp_gb300_obj datatypes
+
+
+class Obj(C.Structure):
+    """hqrrp_gb300_obj: a view (the fields libflame's FLA_Obj exposes)."""
+    _fields_ = [("datatype", C.c_int), ("m", C.c_int), ("n", C.c_int),
+                ("col_stride", C.c_int), ("buffer", C.c_void_p)]
+
 
 class HQRRPError(RuntimeError):
     """A device or shape error reported by libhqrrp_gb300.so."""
@@ -48,6 +56,11 @@ def load():
     L.hqrrp_gb300_dgeqp4_sketch.argtypes = [_ip, _ip, _dp, _ip, _ip, _dp, _dp, _ip, _ip, _dp,
                                             C.c_int]
     L.hqrrp_gb300_dgeqp4_sketch.restype = None
+    L.hqrrp_gb300_ut_blk_var2.argtypes = [Obj, Obj, Obj, C.c_int, C.c_int, C.c_int]
+    L.hqrrp_gb300_ut_blk_var2.restype = C.c_int
+    L.hqrrp_gb300_ut_blk_var2_sketch.argtypes = [Obj, Obj, Obj, C.c_int, C.c_int, C.c_int, _dp,
+                                                 C.c_int]
+    L.hqrrp_gb300_ut_blk_var2_sketch.restype = C.c_int
     L.NoFLA_HQRRP_WY_blk_var4.argtypes = [C.c_int, C.c_int, _dp, C.c_int, _ip, _dp, C.c_int,
                                           C.c_int, C.c_int]
     L.NoFLA_HQRRP_WY_blk_var4.restype = C.c_int
@@ -201,6 +214,31 @@ def hqrrp(A, nb=64, pp=10, panel_pivoting=1, jpvt=None, G=None):
     if rc != 0:
         raise HQRRPError("hqrrp failed (%d): %s" % (rc, last_error()))
     return A, jp, tau[:min(m, n)]
+
+
+def hqrrp_ut(A, nb=64, pp=10, panel_pivoting=1, p=None, G=None):
+    """FLA_HQRRP_UT_blk_var2 (the UT-transform variant) on a copy of A through
+    hqrrp_gb300_ut_blk_var2; returns (A_out, p, s), s the UT scalars
+    (tau_UT = 1 / tau).  p defaults to 1..n and is carried.  G: optional
+    explicit sketch ((nb + pp) x m)."""
+    L = load()
+    A = _fortran(A)
+    m, n = A.shape
+    pv = (np.arange(1, n + 1, dtype=np.int32) if p is None
+          else np.array(p, dtype=np.int32, copy=True))
+    s = np.zeros(max(1, min(m, n)), dtype=np.float64)
+    oA = Obj(DOUBLE, m, n, max(1, m), A.ctypes.data)
+    op = Obj(INT, n, 1, max(1, n), pv.ctypes.data)
+    os_ = Obj(DOUBLE, s.size, 1, s.size, s.ctypes.data)
+    if G is None:
+        rc = L.hqrrp_gb300_ut_blk_var2(oA, op, os_, nb, pp, panel_pivoting)
+    else:
+        Gf = _fortran(G)
+        rc = L.hqrrp_gb300_ut_blk_var2_sketch(oA, op, os_, nb, pp, panel_pivoting,
+                                              Gf.ctypes.data_as(_dp), Gf.shape[0])
+    if rc != 0:
+        raise HQRRPError("hqrrp_ut failed (%d): %s" % (rc, last_error()))
+    return A, pv, s[:min(m, n)]
 
 
 def dgeqp4(A, jpvt=None, lwork=None, G=None):

@@ -55,13 +55,16 @@ size_t hq_skinny_part_elems(const hq_device_info* dev, int mY);
 
 /* ---- Panel: pivoted (or plain) QR of the mp x nc block P (ldp) ---------
  * In place: R on and above the diagonal, Householder vectors below it.
+ * ut != 0: a column whose tail below the diagonal is zero (or empty) gets
+ * the UT transform's reflector H = I - 2 e e^T (tau = 2, beta = -alpha)
+ * instead of LAPACK's H = I (tau = 0).
  * tau[0..nc), U (mp x nc, ldu) = explicit unit-lower copy of the vectors,
  * perm[k] = source column of final column k. */
 int hq_panel_qrp(cudaStream_t stream, const hq_device_info* dev, int mp, int nc, int pivoting,
                  double* P, int ldp, double* tau, double* U, int ldu,
                  int* perm, double* part, size_t part_elems, double* rowbuf, unsigned* bar,
                  int* err, unsigned spin_limit,
-                 int sqnorm);
+                 int sqnorm, int ut);
 size_t hq_panel_part_elems(const hq_device_info* dev, int nc);
 /* Exchange area of the panel kernel for `ctas` CTAs and nc columns, in
  * doubles: [2][ps][ctas] FP64 partials (initial and recomputed norms), then

@@ -181,6 +181,7 @@ typedef struct {
   size_t ws_elems, part_elems;
   prof_rec* prof; /* non-NULL while profiling */
   int mixed;      /* split-BF16 tensor-core block updates */
+  int ut;         /* UT-transform reflector convention in the panels */
   void *ozA, *ozB; /* digit tiles of the two operands of a mixed product */
   int *ozea, *ozeb;
   /* Mixed mode: per global column, the largest FP64 exponent field of the
@@ -680,7 +681,8 @@ static int core_hqrrp_k(hq_ws* w, int m, int n, double* dA, int ldda, int* djpvt
     /* Mixed: squared column norms in the panel's pivoting (division-free
      * LAWN 176 downdate); plain keeps LAPACK's formula. */
     CK(hq_panel_qrp(w->st, dev, mp, b, panel_piv, ABR, ldda, dtau + j, w->U, w->ldu, w->perm,
-                    w->part, w->part_elems, w->rowbuf, w->bar + 1, w->err, spin, w->mixed));
+                    w->part, w->part_elems, w->rowbuf, w->bar + 1, w->err, spin, w->mixed,
+                    w->ut));
     if (w->mixed) CK(hq_set_diag(w->st, b, w->U, w->ldu, 0.0)); /* U' for the digit products */
     /* The panel's swaps on the rows above it and on the labels. */
     CK(hq_permute_cols(w->st, j, AR, ldda, b, w->perm, w->tmp, djpvt + j, w->label_tmp));
@@ -772,11 +774,12 @@ static int ws_begin(hq_ws* w, cudaStream_t user_stream, int use_user) {
 
 /* Host-pointer HQRRP: copy in, factor, copy out. */
 static int hqrrp_host(int m, int n, double* A, int lda, int* jpvt, double* tau, int nb, int pp,
-                      int panel_piv, const double* G, int ldg) {
+                      int panel_piv, const double* G, int ldg, int ut) {
   int rc = check_hqrrp_shape(nb, pp);
   if (rc) return rc;
   hq_ws w;
   if ((rc = ws_begin(&w, NULL, 0))) return rc;
+  w.ut = ut;
   const int mn = imin(m, n), mY = nb + pp, ldda = round_up(m, 32);
   rc = ws_setup(&w, m, n, nb, pp, nb);
   double* dA = rc ? NULL : ws_alloc(&w, sizeof(double) * (size_t)ldda * n);
@@ -828,7 +831,7 @@ HQ_API int NoFLA_HQRRP_WY_blk_var4(int m_A, int n_A, double* buff_A, int ldim_A,
   if (!hqrrp_args_ok(m_A, n_A, ldim_A)) return 0;
   if (imin(m_A, n_A) == 0) return 0;
   return hqrrp_host(m_A, n_A, buff_A, ldim_A, buff_jpvt, buff_tau, nb_alg, pp, panel_pivoting,
-                    NULL, 0);
+                    NULL, 0, 0);
 }
 
 HQ_API int hqrrp_gb300_hqrrp_sketch(int m, int n, double* A, int lda, int* jpvt, double* tau,
@@ -840,7 +843,74 @@ HQ_API int hqrrp_gb300_hqrrp_sketch(int m, int n, double* A, int lda, int* jpvt,
     set_err("explicit sketch missing or ldg < nb + pp");
     return HQ_E_UNSUPPORTED;
   }
-  return hqrrp_host(m, n, A, lda, jpvt, tau, nb, pp, panel_pivoting, G, ldg);
+  return hqrrp_host(m, n, A, lda, jpvt, tau, nb, pp, panel_pivoting, G, ldg, 0);
+}
+
+/* ---- The UT-transform variant behind a libflame-like object API -------- */
+
+/* Element k of a vector view: an n x 1 view (stride 1) or a 1 x n view
+ * (stride col_stride). */
+static size_t obj_vec_stride(const hqrrp_gb300_obj* v) {
+  return v->n == 1 ? 1u : (size_t)v->col_stride;
+}
+
+static int obj_vec_len(const hqrrp_gb300_obj* v) { return v->n == 1 ? v->m : (v->m == 1 ? v->n : -1); }
+
+static int ut_entry(hqrrp_gb300_obj A, hqrrp_gb300_obj p, hqrrp_gb300_obj s, int nb_alg, int pp,
+                    int panel_pivoting, const double* G, int ldg) {
+  g_err[0] = 0;
+  if (A.datatype != HQRRP_GB300_DOUBLE || p.datatype != HQRRP_GB300_INT ||
+      s.datatype != HQRRP_GB300_DOUBLE) {
+    set_err("FLA_HQRRP_UT_blk_var2: A and s must be double, p int objects");
+    return HQ_E_UNSUPPORTED;
+  }
+  const int m = A.m, n = A.n, mn = imin(m, n);
+  if (m < 0 || n < 0 || A.col_stride < imax(1, m) || (mn > 0 && !A.buffer)) {
+    set_err("FLA_HQRRP_UT_blk_var2: invalid A view");
+    return HQ_E_UNSUPPORTED;
+  }
+  if (mn == 0) return 0; /* :179-182 */
+  if (obj_vec_len(&p) < n || obj_vec_len(&s) < mn || !p.buffer || !s.buffer ||
+      (p.n != 1 && p.col_stride < 1) || (s.n != 1 && s.col_stride < 1)) {
+    set_err("FLA_HQRRP_UT_blk_var2: p needs n, s min(m, n) elements (vector views)");
+    return HQ_E_UNSUPPORTED;
+  }
+  int* jp = malloc(sizeof(int) * (size_t)n);
+  double* tau = malloc(sizeof(double) * (size_t)mn);
+  if (!jp || !tau) {
+    free(jp);
+    free(tau);
+    set_err("host allocation failed");
+    return HQ_E_NOMEM;
+  }
+  const size_t ps = obj_vec_stride(&p), ss = obj_vec_stride(&s);
+  for (int k = 0; k < n; ++k) jp[k] = ((const int*)p.buffer)[k * ps];
+  int rc = hqrrp_host(m, n, (double*)A.buffer, A.col_stride, jp, tau, nb_alg, pp, panel_pivoting,
+                      G, ldg, 1);
+  if (!rc) {
+    for (int k = 0; k < n; ++k) ((int*)p.buffer)[k * ps] = jp[k];
+    /* The UT transform's scalar of H = I - u u^T / tau_UT is 1 / tau. */
+    for (int k = 0; k < mn; ++k) ((double*)s.buffer)[k * ss] = 1.0 / tau[k];
+  }
+  free(jp);
+  free(tau);
+  return rc;
+}
+
+HQ_API int hqrrp_gb300_ut_blk_var2(hqrrp_gb300_obj A, hqrrp_gb300_obj p, hqrrp_gb300_obj s,
+                                   int nb_alg, int pp, int panel_pivoting) {
+  return ut_entry(A, p, s, nb_alg, pp, panel_pivoting, NULL, 0);
+}
+
+HQ_API int hqrrp_gb300_ut_blk_var2_sketch(hqrrp_gb300_obj A, hqrrp_gb300_obj p,
+                                          hqrrp_gb300_obj s, int nb_alg, int pp,
+                                          int panel_pivoting, const double* G, int ldg) {
+  if (G == NULL || ldg < nb_alg + pp) {
+    g_err[0] = 0;
+    set_err("explicit sketch missing or ldg < nb + pp");
+    return HQ_E_UNSUPPORTED;
+  }
+  return ut_entry(A, p, s, nb_alg, pp, panel_pivoting, G, ldg);
 }
 
 HQ_API int hqrrp_gb300_hqrrp_device(int m, int n, double* dA, int ldda, int* d_jpvt,
@@ -986,7 +1056,7 @@ static int core_dgeqp4(hq_ws* w, int m, int n, double* dA, int ldda, int* hjp, i
     const int b = imin(FIXED_BLOCK, nf - j), mp = m - j;
     double* ABR = dA + j + (size_t)j * ldda;
     CK(hq_panel_qrp(w->st, dev, mp, b, 0, ABR, ldda, dtau + j, w->U, w->ldu, w->perm, w->part,
-                    w->part_elems, w->rowbuf, w->bar + 1, w->err, spin, 0));
+                    w->part_elems, w->rowbuf, w->bar + 1, w->err, spin, 0, 0));
     if (w->mixed) CK(hq_set_diag(w->st, b, w->U, w->ldu, 0.0)); /* U' for the digit products */
     int rc = block_reflector(w, mp, b, dtau + j, ABR + (size_t)b * ldda, ldda, n - j - b, NULL,
                              NULL);
@@ -1024,7 +1094,7 @@ static int core_dgeqp4(hq_ws* w, int m, int n, double* dA, int ldda, int* hjp, i
                           wtmp, djp + nf, wlab));
     } else if (small) {
       CK(hq_panel_qrp(w->st, dev, mt, nt, 1, At, ldda, dtau + nf, NULL, w->ldu, w->perm,
-                      w->part, w->part_elems, w->rowbuf, w->bar + 1, w->err, spin, 0));
+                      w->part, w->part_elems, w->rowbuf, w->bar + 1, w->err, spin, 0, 0));
       CK(hq_permute_cols(w->st, nf, dA + (size_t)nf * ldda, ldda, nt, w->perm, w->tmp,
                          djp + nf, w->label_tmp));
     } else {

@@ -111,7 +111,7 @@ extern "C" __attribute__((visibility("default"))) int hqrrp_gb300_qrp_noalloc(
   rc = (int)cudaMemsetAsync(err, 0, sizeof(int), st);
   if (rc == 0)
     rc = hq_panel_qrp(st, &dev, m, n, 1, dA, ldda, d_tau, nullptr, 1, perm, part, kPartElems,
-                      rowbuf, bar, err, hq_spin_limit(), 0);
+                      rowbuf, bar, err, hq_spin_limit(), 0, 0);
   if (rc == 0) {
     labels_from_perm<<<(n + 255) / 256, 256, 0, st>>>(perm, n, d_jpvt);
     hq_count_launches(1);

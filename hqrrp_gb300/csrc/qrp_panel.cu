@@ -62,6 +62,7 @@ struct PnArgs {
   unsigned spin_limit;
   int smem_mode, rloc_max, ldxs;
   int sqnorm;  // keep squared norms (d^2 <- d^2 - r^2, LAWN 176's test without divisions)
+  int ut;      // UT-transform convention: a zero tail gives H = I - 2 e e^T (tau 2, beta -alpha)
 };
 
 // Fixed-point stage sums (hq_fixedpoint.h): words 0..2 of a column are the
@@ -244,7 +245,15 @@ __global__ void __launch_bounds__(NT, 1) panel_qrp_kernel(PnArgs a) {
       sw[q] = t;
       srow[q] = r;
       if (q == 0) {
-        const HqReflector h = hq_make_reflector_sq(r, (a.mp - s > 1) ? t : 0.0);
+        const double tail = (a.mp - s > 1) ? t : 0.0;
+        HqReflector h;
+        if (a.ut && tail == 0.0) {  // libflame's Househ2_UT: chi_1 := -chi_1, tau_UT = 1/2
+          h.tau = 2.0;
+          h.beta = -r;
+          h.scale = 1.0;
+        } else {
+          h = hq_make_reflector_sq(r, tail);
+        }
         s_tau = h.tau;
         s_scale = h.scale;
         s_beta = h.beta;
@@ -515,7 +524,7 @@ extern "C" int hq_panel_qrp(cudaStream_t stream, const hq_device_info* dev, int 
                             int pivoting, double* P, int ldp, double* tau,
                             double* U, int ldu, int* perm, double* part, size_t part_elems,
                             double* rowbuf, unsigned* bar, int* err, unsigned spin_limit,
-                            int sqnorm) {
+                            int sqnorm, int ut) {
   if (nc <= 0 || mp <= 0) return 0;
   if (nc > HQ_MAX_PANEL) return (int)cudaErrorInvalidValue;
   PnArgs a;
@@ -536,6 +545,7 @@ extern "C" int hq_panel_qrp(cudaStream_t stream, const hq_device_info* dev, int 
   a.err = err;
   a.spin_limit = spin_limit;
   a.sqnorm = sqnorm;
+  a.ut = ut;
   const int G = panel_grid(dev, mp);
   if (HQ_PANEL_PART_ELEMS(G, nc) > part_elems) return (int)cudaErrorInvalidValue;
   a.acc = reinterpret_cast<unsigned long long*>(part + (size_t)2 * G * a.pstride);

@@ -135,6 +135,37 @@ int hqrrp_gb300_dgeqp4_device(int m, int n, double* dA, int ldda, int* d_jpvt, d
 int hqrrp_gb300_qrp_noalloc(int m, int n, double* dA, int ldda, int* d_jpvt, double* d_tau,
                             void* stream);
 
+/* ---- The UT-transform variant (the reference's second implementation) --
+ * Replaces FLA_HQRRP_UT_blk_var2(FLA_Obj A, FLA_Obj p, FLA_Obj s, int nb_alg,
+ * int pp, int panel_pivoting) of libflame_sources/FLA_HQRRP_UT_blk_var2.h:3-4
+ * (body FLA_HQRRP_UT_blk_var2.c:124-401).  libflame's FLA_Obj is not part of
+ * this library; hqrrp_gb300_obj carries the fields of a view the variant
+ * reads through FLA_Obj_datatype, _length, _width, _col_stride and
+ * _buffer_at_view.  A: m x n double; p: n ints (an n x 1 view, or 1 x n with
+ * col_stride as the element stride), carried like jpvt; s: min(m, n)
+ * doubles, the UT scalars tau_UT of H_k = I - u_k u_k^T / tau_UT (tau_UT =
+ * 1/tau of LAPACK's form; a reflector whose tail below the diagonal is zero
+ * -- always the last one when m <= n -- is H = I - 2 e e^T with tau_UT = 1/2
+ * and that row negated, where LAPACK's convention gives H = I).  Same
+ * pivots, R and reflectors as NoFLA_HQRRP_WY_blk_var4 otherwise (same
+ * algorithm, UT instead of compact-WY block transforms), on the GPU, with the
+ * device Philox sketch; _sketch takes an explicit host sketch G ((nb + pp) x
+ * m, ldg) instead.  Returns 0, or a positive error code (3 for a bad object
+ * or shape) where libflame would abort. */
+#define HQRRP_GB300_DOUBLE 1
+#define HQRRP_GB300_INT 2
+typedef struct hqrrp_gb300_obj {
+  int datatype;   /* HQRRP_GB300_DOUBLE or HQRRP_GB300_INT */
+  int m, n;       /* length (rows) and width (columns) of the view */
+  int col_stride; /* distance between columns, in elements */
+  void* buffer;   /* address of element (0, 0) of the view */
+} hqrrp_gb300_obj;
+int hqrrp_gb300_ut_blk_var2(hqrrp_gb300_obj A, hqrrp_gb300_obj p, hqrrp_gb300_obj s, int nb_alg,
+                            int pp, int panel_pivoting);
+int hqrrp_gb300_ut_blk_var2_sketch(hqrrp_gb300_obj A, hqrrp_gb300_obj p, hqrrp_gb300_obj s,
+                                   int nb_alg, int pp, int panel_pivoting, const double* G,
+                                   int ldg);
+
 /* C = alpha * op(A) op(B) + beta * C in FP64 emulated on the BF16 tensor
  * cores: each operand row (of op(A)) / column (of op(B)) is scaled by a power
  * of two and cut into `slices` 8-bit digits (6 gives about 46 correct bits

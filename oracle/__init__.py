@@ -154,6 +154,11 @@ class Oracle(_Base):
                       C.c_int]
         f.restype = C.c_int
         self._hqrrp_sketch = f
+        f = self.lib.oracle_hqrrp_ut_sketch
+        f.argtypes = [C.c_int, C.c_int, _dp, C.c_int, _ip, _dp, C.c_int, C.c_int, C.c_int, _dp,
+                      C.c_int]
+        f.restype = C.c_int
+        self._hqrrp_ut = f
         for name in ("oracle_dgeqp3",):
             g = getattr(self.lib, name)
             g.argtypes = [_ip, _ip, _dp, _ip, _ip, _dp, _dp, _ip, _ip]
@@ -178,6 +183,24 @@ class Oracle(_Base):
         self._hqrrp_sketch(m, n, _dptr(A), max(1, m), _iptr(jp), _dptr(tau), nb, pp,
                            panel_pivoting, _dptr(G), nb + pp)
         return A, jp, tau[:min(m, n)]
+
+    def hqrrp_ut(self, A, nb=64, pp=10, panel_pivoting=1, p=None, G=None):
+        """The UT-transform variant (FLA_HQRRP_UT_blk_var2) on a copy of A;
+        returns (A_out, p, s) with s the UT scalars.  G: optional explicit sketch."""
+        A = _fortran(A)
+        m, n = A.shape
+        pv = (np.arange(1, n + 1, dtype=np.int32) if p is None
+              else np.array(p, dtype=np.int32, copy=True))
+        s = np.zeros(max(1, min(m, n)), dtype=np.float64)
+        if G is None:
+            self._hqrrp_ut(m, n, _dptr(A), max(1, m), _iptr(pv), _dptr(s), nb, pp,
+                           panel_pivoting, None, 0)
+        else:
+            G = _fortran(G)
+            assert G.shape == (nb + pp, m)
+            self._hqrrp_ut(m, n, _dptr(A), max(1, m), _iptr(pv), _dptr(s), nb, pp,
+                           panel_pivoting, _dptr(G), nb + pp)
+        return A, pv, s[:min(m, n)]
 
     def dgeqp4_sketch(self, A, G, jpvt=None):
         """dgeqp4 whose HQRRP branch uses the sketch G (74 x (m - nf)) in place of

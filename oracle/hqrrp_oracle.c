@@ -77,6 +77,18 @@ typedef int (*fn_ilaenv)(const int*, const char*, const char*, const int*, const
                          const int*, const int*, flen, flen);
 typedef void (*fn_xerbla)(const char*, const int*, flen);
 typedef void (*fn_setthreads)(int);
+typedef void (*fn_dtrsm)(const char*, const char*, const char*, const char*, const int*,
+                         const int*, const double*, const double*, const int*, double*,
+                         const int*, flen, flen, flen, flen);
+typedef void (*fn_dgemv)(const char*, const int*, const int*, const double*, const double*,
+                         const int*, const double*, const int*, const double*, double*,
+                         const int*, flen);
+typedef void (*fn_dger)(const int*, const int*, const double*, const double*, const int*,
+                        const double*, const int*, double*, const int*);
+typedef void (*fn_dcopy)(const int*, const double*, const int*, double*, const int*);
+typedef void (*fn_daxpy)(const int*, const double*, const double*, const int*, double*,
+                         const int*);
+typedef void (*fn_dscal)(const int*, const double*, double*, const int*);
 
 static struct {
   void* handle;
@@ -98,6 +110,13 @@ static struct {
   fn_ilaenv ilaenv;
   fn_xerbla xerbla;
   fn_setthreads set_threads;
+  /* used by the UT-variant restatement */
+  fn_dtrsm dtrsm;
+  fn_dgemv dgemv;
+  fn_dger dger;
+  fn_dcopy dcopy;
+  fn_daxpy daxpy;
+  fn_dscal dscal;
 } LA;
 
 static void* find_sym(void* h, const char* prefix, const char* base) {
@@ -132,11 +151,18 @@ int oracle_open(const char* path) {
     LOAD(dormqr, "dormqr_");
     LOAD(ilaenv, "ilaenv_");
     LOAD(xerbla, "xerbla_");
+    LOAD(dtrsm, "dtrsm_");
+    LOAD(dgemv, "dgemv_");
+    LOAD(dger, "dger_");
+    LOAD(dcopy, "dcopy_");
+    LOAD(daxpy, "daxpy_");
+    LOAD(dscal, "dscal_");
 #undef LOAD
     LA.set_threads = (fn_setthreads)find_sym(h, p, "openblas_set_num_threads");
     if (LA.dgemm && LA.dlacpy && LA.dlarfg && LA.dlarf && LA.dlarft && LA.dlarfb &&
         LA.dtrmm && LA.idamax && LA.dswap && LA.dnrm2 && LA.dlamch && LA.dgeqpf &&
-        LA.dgeqp3 && LA.dgeqrf && LA.dormqr && LA.ilaenv && LA.xerbla) {
+        LA.dgeqp3 && LA.dgeqrf && LA.dormqr && LA.ilaenv && LA.xerbla && LA.dtrsm &&
+        LA.dgemv && LA.dger && LA.dcopy && LA.daxpy && LA.dscal) {
       LA.handle = h;
       return 0;
     }
@@ -557,4 +583,262 @@ void oracle_dgeqp3(int* m, int* n, double* A, int* lda, int* jpvt, double* tau, 
 void oracle_dgeqpf(int* m, int* n, double* A, int* lda, int* jpvt, double* tau, double* work,
                    int* info) {
   LA.dgeqpf(m, n, A, lda, jpvt, tau, work, info);
+}
+
+/* ======================================================================== */
+/* The reference's second implementation: the UT-transform variant         */
+/* libflame_sources/FLA_HQRRP_UT_blk_var2.c:124-401 (helpers :405-1166),    */
+/* restated over plain column-major buffers (its libflame objects are views */
+/* of such buffers).  libflame itself is not part of the reference tree and */
+/* is not installed here, so this restatement is not pinned to a compiled   */
+/* reference: it is checked against the WY restatement above (same pivots,  */
+/* the same R up to the sign convention below, s = 1 / tau) in             */
+/* tests/test_oracle.py.                                                    */
+/*                                                                          */
+/* Third-party routine restated: libflame's FLA_Househ2_UT_l_opd (libflame  */
+/* 5.x, src/base/flamec/util/lapack/), called at :764.  For x = [chi_1; x2] */
+/* it returns u2 = x2 / (chi_1 - alpha), alpha = -sign(chi_1) ||x||_2       */
+/* written over chi_1, and tau = (1 + u2^T u2) / 2, so H = I - u u^T / tau, */
+/* u = [1; u2]; when x2 = 0 it sets chi_1 = -chi_1 and tau = 1/2 (H         */
+/* reflects e_1), where LAPACK's dlarfg returns tau = 0 (H = I).           */
+
+static struct {
+  int have_spare;
+  double spare;
+} polar_ut; /* MyFLA_Normal_random_number's own carried value (:443-465) */
+
+static double polar_normal_ut(void) {
+  if (polar_ut.have_spare) {
+    polar_ut.have_spare = 0;
+    return polar_ut.spare;
+  }
+  double u, v, r;
+  do {
+    u = -1.0 + 2.0 * ((double)rand() / RAND_MAX);
+    v = -1.0 + 2.0 * ((double)rand() / RAND_MAX);
+    r = u * u + v * v;
+  } while (r == 0 || r >= 1);
+  double f = sqrt((-2 * log(r)) / r);
+  polar_ut.spare = v * f;
+  polar_ut.have_spare = 1;
+  return u * f;
+}
+
+static void househ2_ut(int m_x2, double* chi_1, double* x2, double* tau) {
+  const int one = 1, two = 2;
+  const double norm_x2 = m_x2 > 0 ? LA.dnrm2(&m_x2, x2, &one) : 0.0;
+  if (norm_x2 == 0.0) {
+    *chi_1 = -*chi_1;
+    *tau = 0.5;
+    return;
+  }
+  double v[2] = {fabs(*chi_1), norm_x2};
+  const double norm_x = LA.dnrm2(&two, v, &one);
+  const double alpha = (*chi_1 >= 0.0 ? -1.0 : 1.0) * norm_x;
+  const double cma = *chi_1 - alpha;
+  const double inv = 1.0 / cma;
+  LA.dscal(&m_x2, &inv, x2, &one);
+  const double nu = norm_x2 / fabs(cma); /* ||u2|| */
+  *tau = (1.0 + nu * nu) / 2.0;
+  *chi_1 = alpha;
+}
+
+/* MyFLA_Apply_H2_UT_l_opd_var2 (:824-930): w = (a1t + A2^T u2) / tau,
+ * a1t -= w, A2 -= u2 w^T. */
+static void apply_h2_ut(int m2, int n1, double tau, const double* u2, double* a1t, int inc_a1t,
+                        double* A2, int lda2, double* w) {
+  const int one = 1;
+  const double d_one = 1.0, m_one = -1.0;
+  if (n1 == 0) return;
+  LA.dcopy(&n1, a1t, &inc_a1t, w, &one);
+  LA.dgemv("Transpose", &m2, &n1, &d_one, A2, &lda2, u2, &one, &d_one, w, &one, 9);
+  const double rtau = 1.0 / tau;
+  LA.dscal(&n1, &rtau, w, &one);
+  LA.daxpy(&n1, &m_one, w, &one, a1t, &inc_a1t);
+  LA.dger(&m2, &n1, &m_one, u2, &one, w, &one, A2, &lda2);
+}
+
+/* NoFLA_my_idamax (:1123-1166): first index of the largest |d|, strict <. */
+static int my_idamax(int n, const double* d) {
+  if (n < 1) return -1;
+  int r = 0;
+  double dmax = fabs(d[0]);
+  for (int i = 1; i < n; ++i)
+    if (dmax < fabs(d[i])) {
+      r = i;
+      dmax = fabs(d[i]);
+    }
+  return r;
+}
+
+/* MyFLA_QRPmod_UT_unb_var2 (:640-822). */
+static void qrp_ut_unblocked(int pivoting, int stages, int m, int n, double* A, int lda,
+                             int* p, double* t, companion* B, companion* C, double* T,
+                             int ldt) {
+  const int one = 1;
+  const double d_one = 1.0;
+  const int mn = m < n ? m : n;
+  if (stages < 0) stages = mn;
+  double* d = malloc(sizeof(double) * (n > 0 ? n : 1));
+  double* e = malloc(sizeof(double) * (n > 0 ? n : 1));
+  double* work = malloc(sizeof(double) * (n > 0 ? n : 1));
+  if (pivoting == 1) colnorms(m, n, A, lda, d, e);
+  for (int j = 0; j < stages; ++j) {
+    if (pivoting == 1) {
+      const int idx = my_idamax(n - j, d + j);
+      companion bk, ck, *pb = NULL, *pc = NULL;
+      if (B) { bk = *B; bk.a = B->a + (size_t)j * B->ld; pb = &bk; }
+      if (C) { ck = *C; ck.a = C->a + (size_t)j * C->ld; pc = &ck; }
+      bring_to_front(idx, m, A + (size_t)j * lda, lda, pb, pc, p + j, d + j, e + j);
+    }
+    const int m21 = m - j - 1, n22 = n - j - 1;
+    double* ajj = A + j + (size_t)j * lda;
+    househ2_ut(m21, ajj, ajj + 1, t + j);
+    apply_h2_ut(m21, n22, t[j], ajj + 1, ajj + lda, lda, ajj + 1 + lda, lda, work);
+    if (T) {
+      /* T[j, j] = tau_j; T[0:j, j] = A[j, 0:j]^T + A[j+1:, 0:j]^T u21. */
+      T[j + (size_t)j * ldt] = t[j];
+      LA.dcopy(&j, A + j, &lda, T + (size_t)j * ldt, &one);
+      LA.dgemv("Transpose", &m21, &j, &d_one, A + j + 1, &lda, ajj + 1, &one, &d_one,
+               T + (size_t)j * ldt, &one, 9);
+    }
+    if (pivoting == 1)
+      colnorms_downdate(m21, n22, d + j + 1, e + j + 1, ajj + lda, lda, ajj + 1 + lda, lda);
+  }
+  free(d);
+  free(e);
+  free(work);
+}
+
+/* MyFLA_Apply_Q_UT_lhfc_blk_var2 (:532-582): [B1; B2] := Q^T [B1; B2] with
+ * Q = I - U inv(T) U^T, U = [U11 (unit lower); U21]. */
+static void apply_q_ut_lhfc(int b, int mr, int nc, const double* U11, const double* U21, int ldu,
+                            const double* T, int ldt, double* B1, double* B2, int ldb) {
+  if (nc <= 0) return;
+  const double d_one = 1.0, m_one = -1.0;
+  double* W = malloc(sizeof(double) * (size_t)b * nc);
+  LA.dlacpy("All", &b, &nc, B1, &ldb, W, &b, 3);
+  LA.dtrmm("Left", "Lower", "Transpose", "Unit", &b, &nc, &d_one, U11, &ldu, W, &b, 4, 5, 9, 4);
+  if (mr > 0)
+    LA.dgemm("Transpose", "No transpose", &b, &nc, &mr, &d_one, U21, &ldu, B2, &ldb, &d_one, W,
+             &b, 9, 12);
+  LA.dtrsm("Left", "Upper", "Transpose", "Non-unit", &b, &nc, &d_one, T, &ldt, W, &b, 4, 5, 9,
+           8);
+  if (mr > 0)
+    LA.dgemm("No transpose", "No transpose", &mr, &nc, &b, &m_one, U21, &ldu, W, &b, &d_one, B2,
+             &ldb, 12, 12);
+  LA.dtrmm("Left", "Lower", "No transpose", "Unit", &b, &nc, &m_one, U11, &ldu, W, &b, 4, 5, 12,
+           4);
+  for (int c = 0; c < nc; ++c)
+    for (int r = 0; r < b; ++r) B1[r + (size_t)c * ldb] += W[r + (size_t)c * b];
+  free(W);
+}
+
+/* MyFLA_Apply_Q_UT_rnfc_blk_var2 (:585-637): [B1, B2] := [B1, B2] Q. */
+static void apply_q_ut_rnfc(int b, int mr, int rows, const double* U11, const double* U21,
+                            int ldu, const double* T, int ldt, double* B1, double* B2, int ldb) {
+  const double d_one = 1.0, m_one = -1.0;
+  double* W = malloc(sizeof(double) * (size_t)b * (rows > 0 ? rows : 1));
+  for (int c = 0; c < b; ++c)
+    for (int r = 0; r < rows; ++r) W[c + (size_t)r * b] = B1[r + (size_t)c * ldb];
+  LA.dtrmm("Left", "Lower", "Transpose", "Unit", &b, &rows, &d_one, U11, &ldu, W, &b, 4, 5, 9,
+           4);
+  if (mr > 0)
+    LA.dgemm("Transpose", "Transpose", &b, &rows, &mr, &d_one, U21, &ldu, B2, &ldb, &d_one, W, &b,
+             9, 9);
+  LA.dtrsm("Left", "Upper", "Transpose", "Non-unit", &b, &rows, &d_one, T, &ldt, W, &b, 4, 5, 9,
+           8);
+  if (mr > 0)
+    LA.dgemm("Transpose", "Transpose", &rows, &mr, &b, &m_one, W, &b, U21, &ldu, &d_one, B2, &ldb,
+             9, 9);
+  LA.dtrmm("Left", "Lower", "No transpose", "Unit", &b, &rows, &m_one, U11, &ldu, W, &b, 4, 5,
+           12, 4);
+  for (int c = 0; c < b; ++c)
+    for (int r = 0; r < rows; ++r) B1[r + (size_t)c * ldb] += W[c + (size_t)r * b];
+  free(W);
+}
+
+/* MyFLA_Downdate_Y (:468-529):
+ * Y2 -= (G1 - (G1 U11 + G2 U21) inv(T) U11^T) R12, then G := G Q. */
+static void downdate_y_ut(int b, int mr, int mY, int n2, const double* U11, const double* U21,
+                          int ldu, const double* A12, int lda, const double* T, int ldt,
+                          double* Y2, int ldy, double* G1, double* G2, int ldg) {
+  const double d_one = 1.0, m_one = -1.0;
+  double* B = malloc(sizeof(double) * (size_t)mY * b);
+  LA.dlacpy("All", &mY, &b, G1, &ldg, B, &mY, 3);
+  LA.dtrmm("Right", "Lower", "No transpose", "Unit", &mY, &b, &d_one, U11, &ldu, B, &mY, 5, 5,
+           12, 4);
+  if (mr > 0)
+    LA.dgemm("No transpose", "No transpose", &mY, &b, &mr, &d_one, G2, &ldg, U21, &ldu, &d_one,
+             B, &mY, 12, 12);
+  LA.dtrsm("Right", "Upper", "No transpose", "Non-unit", &mY, &b, &d_one, T, &ldt, B, &mY, 5, 5,
+           12, 8);
+  LA.dtrmm("Right", "Lower", "Transpose", "Unit", &mY, &b, &m_one, U11, &ldu, B, &mY, 5, 5, 9,
+           4);
+  for (int c = 0; c < b; ++c)
+    for (int r = 0; r < mY; ++r) B[r + (size_t)c * mY] += G1[r + (size_t)c * ldg];
+  if (n2 > 0)
+    LA.dgemm("No transpose", "No transpose", &mY, &n2, &b, &m_one, B, &mY, A12, &lda, &d_one, Y2,
+             &ldy, 12, 12);
+  apply_q_ut_rnfc(b, mr, mY, U11, U21, ldu, T, ldt, G1, G2, ldg);
+  free(B);
+}
+
+/* FLA_HQRRP_UT_blk_var2 (:124-401): p carried (permuted like the columns),
+ * s[0..min(m,n)) the UT scalars tau_UT.  G_in (optional, (nb+pp) x m, ld
+ * ldg_in) replaces the drawn sketch. */
+int oracle_hqrrp_ut_sketch(int m, int n, double* A, int lda, int* p, double* s, int nb, int pp,
+                           int panel_piv, const double* G_in, int ldg_in) {
+  const int mn = imin(m, n);
+  if (mn <= 0) return 0;
+  srand(12);
+  const int mY = nb + pp, ldg = mY, ldy = mY, ldw = nb;
+  double* G = malloc(sizeof(double) * (size_t)mY * m);
+  double* Y = malloc(sizeof(double) * (size_t)mY * n);
+  double* V = malloc(sizeof(double) * (size_t)mY * n);
+  double* W = calloc((size_t)nb * n, sizeof(double));
+  if (G_in) {
+    for (int c = 0; c < m; ++c)
+      memcpy(G + (size_t)c * ldg, G_in + (size_t)c * ldg_in, sizeof(double) * mY);
+  } else {
+    for (int c = 0; c < m; ++c)
+      for (int r = 0; r < mY; ++r) G[r + (size_t)c * ldg] = polar_normal_ut();
+  }
+  {
+    const double one = 1.0, zero = 0.0;
+    LA.dgemm("No transpose", "No transpose", &mY, &n, &m, &one, G, &ldg, A, &lda, &zero, Y, &ldy,
+             12, 12);
+  }
+  for (int j = 0; j < mn;) {
+    const int b = imin(imin(m - j, n - j), nb);
+    const int last = imin(m - j - b, n - j - b) <= 0;
+    double* AR = A + (size_t)j * lda;
+    double* ABR = AR + j;
+    double* YR = Y + (size_t)j * ldy;
+    double* T1 = W + (size_t)j * ldw;
+    if (!last) {
+      const int nvr = n - j;
+      double* VR = V + (size_t)j * ldy;
+      LA.dlacpy("All", &mY, &nvr, YR, &ldy, VR, &ldy, 3);
+      companion ca = {AR, m, lda}, cy = {YR, mY, ldy};
+      qrp_ut_unblocked(1, b, mY, nvr, VR, ldy, p + j, s + j, &ca, &cy, NULL, 0);
+    }
+    {
+      companion ca = {AR, j, lda}, cy = {YR, mY, ldy};
+      qrp_ut_unblocked(panel_piv, -1, m - j, b, ABR, lda, p + j, s + j, &ca, &cy, T1, ldw);
+    }
+    const int n2 = n - j - b, mr = m - j - b;
+    double* A12 = ABR + (size_t)b * lda;
+    if (n2 > 0)
+      apply_q_ut_lhfc(b, mr, n2, ABR, ABR + b, lda, T1, ldw, A12, A12 + b, lda);
+    if (n2 > 0)
+      downdate_y_ut(b, mr, mY, n2, ABR, ABR + b, lda, A12, lda, T1, ldw, YR + (size_t)b * ldy,
+                    ldy, G + (size_t)j * ldg, G + (size_t)(j + b) * ldg, ldg);
+    j += b;
+  }
+  free(G);
+  free(Y);
+  free(V);
+  free(W);
+  return 0;
 }

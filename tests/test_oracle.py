@@ -116,3 +116,42 @@ def test_oracle_quality(oracle_lib):
     assert res < 1e-14 and orth < 1e-13
     ratio = d / sigma  # rank-revealing: |R_kk| tracks sigma_k
     assert 0.05 < ratio.min() and ratio.max() < 20
+
+
+@pytest.mark.parametrize("m,n,nb,pp,ppiv", [(300, 280, 32, 10, 1), (150, 260, 32, 10, 1),
+                                            (400, 300, 32, 8, 0), (257, 257, 64, 10, 1),
+                                            (700, 350, 48, 10, 1)])
+def test_ut_restatement_agrees_with_wy(oracle_lib, m, n, nb, pp, ppiv):
+    """The UT-variant restatement (FLA_HQRRP_UT_blk_var2; libflame is absent,
+    so it cannot be compiled) against the WY restatement pinned to the
+    reference: on the same sketch the same pivots, the same factored matrix up
+    to rounding, s = 1 / tau -- except where the UT transform's convention
+    differs: a reflector with an empty or zero tail is H = I - 2 e e^T (tau_UT
+    = 1/2, the row negated) where LAPACK's is H = I.  In a matrix with
+    m <= n that is the last row (stage m - 1)."""
+    A = oracle.gaussian(m, n, m + n + nb)
+    G = oracle_lib.sketch(nb + pp, m)
+    Aw, jw, tw = oracle_lib.hqrrp_sketch(A, G, nb, pp, ppiv)
+    Au, ju, su = oracle_lib.hqrrp_ut(A, nb, pp, ppiv, G=G)
+    np.testing.assert_array_equal(ju, jw)
+    k = min(m, n)
+    Aw = Aw.copy()
+    tw = tw.copy()
+    if m <= n:  # the empty-tail reflector of the last row
+        assert tw[k - 1] == 0.0 and su[k - 1] == 0.5
+        Aw[k - 1, k - 1:] *= -1.0
+        tw[k - 1] = 2.0
+    assert np.max(np.abs(su * tw - 1.0)) <= 1e-12
+    den = np.linalg.norm(Aw, axis=0)
+    assert np.max(np.linalg.norm(Au - Aw, axis=0) / den) <= 1e-12
+
+
+def test_ut_restatement_drawn_sketch_is_the_reference_sketch(oracle_lib):
+    """MyFLA_Normal_random_matrix draws the same polar-method stream after
+    srand(12) as the WY variant's generator (for an even count)."""
+    A = oracle.gaussian(200, 150, 3)
+    G = oracle_lib.sketch(42, 200)
+    a = oracle_lib.hqrrp_ut(A, 32, 10, 1)
+    b = oracle_lib.hqrrp_ut(A, 32, 10, 1, G=G)
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x, y)
