@@ -514,6 +514,46 @@ __global__ void larft_kernel(int k, const double* __restrict__ Z, int ldz,
       T[(e % k) + (size_t)(e / k) * ldt] = sT[(e % k) + (size_t)(e / k) * ld];
 }
 
+// The same T, one CTA per row.  Row r of T only involves row r itself:
+// T[r, i] = -tau_i * sum_{c = r}^{i-1} T[r, c] Z[c, i] for i > r, T[r, r] =
+// tau_r (zero when tau_i = 0), so the k rows are independent recurrences and
+// run side by side on k SMs instead of one SM's FP64 pipe doing all of them.
+// The CTA first stages the part of Z its row reads (Z[r:i, i], i > r: the
+// upper triangle from row r) in shared memory with all its threads, then one
+// warp runs the recurrence: per step a dot of length i - r over the lanes and
+// a shuffle reduction, with the row kept in shared memory.
+constexpr int LARFT_ROW_MAX = 128;  // k up to this: row and staged triangle fit (<= 66 KB)
+
+__global__ void __launch_bounds__(128) larft_rows_kernel(int k, const double* __restrict__ Z,
+                                                         int ldz, const double* __restrict__ tau,
+                                                         double* __restrict__ T, int ldt) {
+  extern __shared__ double lsm[];
+  double* sT = lsm;      // [k] the row, from column r on
+  double* sZ = lsm + k;  // [k (k - 1) / 2] the staged triangle
+  const int r = blockIdx.x, tid = threadIdx.x, lane = tid & 31;
+  // Column i > r of the staged triangle holds Z[r:i, i] at offset
+  // off(i) = (i - r - 1)(i - r) / 2.
+  for (int i = r + 1; i < k; ++i) {
+    const int off = (i - r - 1) * (i - r) / 2;
+    for (int c = r + tid; c < i; c += blockDim.x) sZ[off + (c - r)] = Z[c + (size_t)i * ldz];
+  }
+  __syncthreads();
+  if (tid < 32) {
+    if (lane == 0) sT[0] = tau[r];
+    __syncwarp();
+    for (int i = r + 1; i < k; ++i) {
+      const double ti = tau[i];
+      const int off = (i - r - 1) * (i - r) / 2;
+      double acc = 0.0;
+      for (int c = lane; c < i - r; c += 32) acc = fma(sT[c], sZ[off + c], acc);
+      acc = hq_warp_sum(acc);
+      if (lane == 0) sT[i - r] = ti != 0.0 ? -ti * acc : 0.0;
+      __syncwarp();
+    }
+    for (int i = lane; i < k; i += 32) T[r + (size_t)i * ldt] = i < r ? 0.0 : sT[i - r];
+  }
+}
+
 }  // namespace
 
 extern "C" size_t hq_panel_part_elems(const hq_device_info* dev, int nc) {
@@ -577,6 +617,15 @@ extern "C" int hq_larft_from_gram(cudaStream_t stream, int k, const double* Z, i
                                   const double* tau, double* T, int ldt) {
   if (k <= 0) return 0;
   if (k > HQ_MAX_MY) return (int)cudaErrorInvalidValue;
+  if (k <= LARFT_ROW_MAX) {
+    const size_t rsm = sizeof(double) * ((size_t)k + (size_t)k * (k - 1) / 2);
+    cudaError_t e = cudaFuncSetAttribute(larft_rows_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsm);
+    if (e != cudaSuccess) return (int)e;
+    larft_rows_kernel<<<k, 128, rsm, stream>>>(k, Z, ldz, tau, T, ldt);
+    hq_count_launches(1);
+    return (int)cudaGetLastError();
+  }
   const size_t smem = sizeof(double) * (size_t)k * (k | 1);
   if (smem <= 160 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(larft_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
