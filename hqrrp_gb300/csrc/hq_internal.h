@@ -122,6 +122,13 @@ int hq_ozk_gemm(cudaStream_t stream, const hq_device_info* dev, int M, int N, in
                 const void* Atiles, const int* ea, const void* Btiles, const int* eb, int mode,
                 double sign, double* C, long long crs, long long ccs, double* ws,
                 size_t ws_elems, int* err, unsigned spin_limit);
+/* mode 0 product whose N side is FP64: Y element (n, k) at Y[n*yld + k],
+ * raw[n] its row's largest exponent field; digits are cut on the fly (S = 7).
+ * cudaErrorNotSupported when Y's alignment does not allow tensor-map loads. */
+int hq_ozk_gemm_c64(cudaStream_t stream, const hq_device_info* dev, int M, int N, int K,
+                    const void* Atiles, const int* ea, const double* Y, long long yld,
+                    const int* raw, double sign, double* C, long long crs, long long ccs,
+                    double* ws, size_t ws_elems, int* err, unsigned spin_limit);
 /* K <= 256: persistent kernel with double-buffered TMEM; the N side must be
  * split with side 2 (32-row tiles).  Mode 1 with colexp: colexp[c] (zeroed
  * before) receives the largest exponent field of the new C(r, c) over rows

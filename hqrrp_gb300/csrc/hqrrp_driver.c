@@ -593,8 +593,25 @@ static int block_reflector(hq_ws* w, int mp, int b, const double* tau, double* C
     /* W1 = U^T C, W2 = T^T W1 and C -= U W2 on the tensor cores. */
     /* cx_in: C's columns' largest exponent fields (from the previous update);
      * cx_out: the same for the next block, over rows >= b of the new C. */
-    int rc = ozk_product_x(w, OZK_SLICES, b, nc2, mp, w->U, w->ldu, 1, Cm, ldc, 1, 0, 1.0,
-                           w->W1, 1, w->ldw, cx_in, NULL, 0, w->ozUT, w->ozUTe);
+    int rc = HQ_OK, done = 0;
+    /* HQRRP_GB300_SPLIT_TRAILING=1 keeps the separate split pass (the same
+     * digits; for verification). */
+    const char* split_env = getenv("HQRRP_GB300_SPLIT_TRAILING");
+    if (cx_in && !(split_env && split_env[0] == '1')) {
+      /* C's column exponents are known: the product reads C as FP64 and cuts
+       * it into digits on the fly (no split pass over the trailing matrix). */
+      const int e = hq_ozk_gemm_c64(w->st, &w->ds->dev, b, nc2, mp, w->ozUT, w->ozUTe, Cm, ldc,
+                                    cx_in, 1.0, w->W1, 1, w->ldw, w->ws, w->ws_elems, w->err,
+                                    spin_limit());
+      if (e != (int)cudaErrorNotSupported) {
+        CK(e);
+        prof_mark(w, PH_TENSOR, (double)OZK_SLICES * (OZK_SLICES + 1) * b * nc2 * (double)mp);
+        done = 1;
+      }
+    }
+    if (!done)
+      rc = ozk_product_x(w, OZK_SLICES, b, nc2, mp, w->U, w->ldu, 1, Cm, ldc, 1, 0, 1.0, w->W1, 1,
+                         w->ldw, cx_in, NULL, 0, w->ozUT, w->ozUTe);
     if (rc) return rc;
     CK(hq_add_matrix(w->st, b, nc2, 1.0, Cm, ldc, w->W1, w->ldw));
     CK(cudaStreamWaitEvent(w->st, w->ev_t, 0));

@@ -380,7 +380,14 @@ struct OzkArgs {
   // of the new C over rows >= row_lo of column c (atomicMax; zeroed before).
   int* colexp;
   int row_lo;
+  // FP64 N-side operand (ozk_gemm_c64_kernel): eb_raw[n] is column n's
+  // largest exponent field, from which its scale exponent follows (eb unused).
+  const int* eb_raw;
 };
+
+// The scale exponent of a row whose largest exponent field is raw: 2^e >
+// max |x| >= 2^(e-1), 0 for a zero row.
+__device__ __forceinline__ int scale_of_raw(int raw) { return raw == 0 ? 0 : raw - 1022; }
 
 __device__ __forceinline__ void mbar_init(uint64_t* b, unsigned count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count));
@@ -525,7 +532,7 @@ __device__ __forceinline__ void write_row(const OzkArgs& a, int r, int n0, doubl
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       const int n = n0 + c8 + j;
-      ek[j] = (live && n < a.N) ? er + a.eb[n] : 0;
+      ek[j] = (live && n < a.N) ? er + (a.eb_raw ? scale_of_raw(a.eb_raw[n]) : a.eb[n]) : 0;
       cv[j] = (a.mode == 1 && live && n < a.N) ? crow[(long long)n * a.ccs] : 0.0;
     }
     unsigned fx[8];
@@ -747,6 +754,253 @@ __global__ void __launch_bounds__(NT, 1) ozk_gemm_kernel(OzkArgs a,
       // done_bar was committed after the loop; its completion covers all MMAs.
       mbar_wait(&done_bar, 0, lim, nullptr);
     }
+    __syncthreads();
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase),
+                 "r"(tmem_cols)
+                 : "memory");
+}
+
+// Long-K product whose N-side operand is read as FP64 (C in the block update
+// W1 = U'^T C): the producer brings each K block of C (80 columns x 32 rows,
+// 20 KB) with a 2-D tensor-map load next to the M side's digit tiles, and the
+// epilogue warps -- idle between drains -- cut it into the seven digit planes
+// in shared memory, in the 64-byte-swizzled layout the MMA descriptors read
+// (16-byte chunk c of row r of a 64-byte row at chunk c ^ ((r >> 1) & 3)).
+// The column scales come from eb_raw (each column's largest exponent field,
+// recorded by the epilogue of the update that wrote C), so nothing is read
+// twice: the trailing matrix is read once as FP64 instead of being split to
+// 14 bytes of digits per entry and read back.  The digits are those
+// ozk_split_chunk_kernel writes.  A conversion barrier per stage orders the
+// digit writes (generic proxy, fenced to the async proxy) before the MMAs.
+constexpr int C64_TILE = TN * TK * 8;  // 20 KB of FP64 per stage
+
+// One thread's share of a block's conversion: 4 consecutive K entries (h-th
+// quarter of the 32) of tile column c, read as two 16-byte loads, written as
+// 8 bytes of each digit plane.
+template <int S>
+__device__ __forceinline__ void convert_quarter(const double* __restrict__ sC, uint8_t* sBst, int c,
+                                                int h, int shift_base) {
+  constexpr unsigned long long BIAS = 0x8080808080808080ULL >> (8 * (8 - S));
+  const double2* x2 = reinterpret_cast<const double2*>(sC + c * TK + h * 4);
+  const double2 p0 = x2[0], p1 = x2[1];
+  const double x[4] = {p0.x, p0.y, p1.x, p1.y};
+  unsigned long long W[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) W[j] = (unsigned long long)fixed_point(x[j], shift_base) + BIAS;
+  const int phys = (h >> 1) ^ ((c >> 1) & 3);  // 64-byte swizzle of the 16-byte chunk
+  uint8_t* dst = sBst + c * (TK * 2) + phys * 16 + (h & 1) * 8;
+#pragma unroll
+  for (int s = 0; s < S; ++s) {
+    const int p = S - 1 - s;
+    uint32_t w[2];
+#pragma unroll
+    for (int j = 0; j < 4; j += 2) {
+      uint32_t u0, u1;
+      if (p == S - 1) {
+        u0 = (uint32_t)(W[j] >> (8 * p));
+        u1 = (uint32_t)(W[j + 1] >> (8 * p));
+      } else {
+        u0 = (uint32_t)(W[j] >> (8 * p)) & 255u;
+        u1 = (uint32_t)(W[j + 1] >> (8 * p)) & 255u;
+      }
+      w[j >> 1] = __byte_perm(digit_scaled(u0, s), digit_scaled(u1, s), 0x7632);
+    }
+    *reinterpret_cast<uint2*>(dst + s * B_TILE) = make_uint2(w[0], w[1]);
+  }
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__global__ void __launch_bounds__(NT, 1) ozk_gemm_c64_kernel(
+    OzkArgs a, const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmC) {
+  constexpr int S = 7;
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  // a_full: the M side's digits of a block landed; c_full: its FP64 N-side
+  // tile landed; c_empty: the converters are done with that FP64 tile;
+  // conv_bar: its digits are in the B stage; empty_bar: the MMAs are done
+  // with the A and B stages.  The FP64 tile of block i is fetched as soon as
+  // block i - 2's was converted, so its load never waits for the MMAs.
+  __shared__ __align__(8) uint64_t a_full[MAX_STAGES], c_full[MAX_STAGES], c_empty[MAX_STAGES],
+      empty_bar[MAX_STAGES], conv_bar[MAX_STAGES];
+  __shared__ __align__(8) uint64_t drain_full, drain_empty, done_bar;
+  __shared__ uint32_t tmem_base;
+  __shared__ volatile int s_abort;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int a_stage = S * A_TILE, b_stage = S * B_TILE;
+  const int nacc = n_acc(S);
+  const uint32_t tmem_cols = tmem_pow2((uint32_t)(nacc * TN));
+  uint8_t* smem = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);
+  const int STAGES = a.stages;
+  uint8_t* sA = smem;
+  uint8_t* sB = smem + STAGES * a_stage;
+  uint8_t* sC = sB + STAGES * b_stage;  // FP64 staging, C64_TILE per stage
+  const int mt = blockIdx.x, nt = blockIdx.y, z = blockIdx.z;
+  const int kb0 = z * a.kb_per_z;
+  const int nkb = min(a.KB - kb0, a.kb_per_z);
+  const int ndrain = nkb > 0 ? (nkb - 1) / KB_PER_DRAIN : 0;
+
+  if (tid == 0) {
+    for (int i = 0; i < STAGES; ++i) {
+      mbar_init(&a_full[i], 1);
+      mbar_init(&c_full[i], 1);
+      mbar_init(&c_empty[i], NEPI);
+      mbar_init(&empty_bar[i], 1);
+      mbar_init(&conv_bar[i], NEPI);
+    }
+    mbar_init(&drain_full, 1);
+    mbar_init(&drain_empty, NEPI);
+    mbar_init(&done_bar, 1);
+    s_abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_base)),
+                 "r"(tmem_cols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tbase = tmem_base;
+  const unsigned lim = a.spin_limit;
+  int mma_issued = 0;
+  int a_issued = 0, c_issued = 0;  // producer lanes 0 and 1
+
+  if (warp == PRODUCER_WARP) {
+    if (lane == 0) {  // the M side's digit tiles, as the MMAs free the stages
+      for (int i = 0; i < nkb; ++i) {
+        const int st = i % STAGES;
+        if (!mbar_wait(&empty_bar[st], ((i / STAGES) & 1) ^ 1, lim, &s_abort)) {
+          s_abort = 1;
+          break;
+        }
+        mbar_expect_tx(&a_full[st], (unsigned)a_stage);
+        tma_load_3d(sA + st * a_stage, &tmA, (kb0 + i) * TK, mt * TM, 0, &a_full[st]);
+        ++a_issued;
+      }
+    } else if (lane == 1) {  // the FP64 tiles, as the converters free them
+      for (int i = 0; i < nkb; ++i) {
+        const int st = i % STAGES;
+        if (!mbar_wait(&c_empty[st], ((i / STAGES) & 1) ^ 1, lim, &s_abort)) {
+          s_abort = 1;
+          break;
+        }
+        mbar_expect_tx(&c_full[st], (unsigned)C64_TILE);
+        tma_load_2d(sC + st * C64_TILE, &tmC, (kb0 + i) * TK, nt * TN, &c_full[st]);
+        ++c_issued;
+      }
+    }
+  } else if (warp == MMA_WARP) {
+    if (lane == 0) {
+      const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TN >> 3) << 17) |
+                             ((uint32_t)(TM >> 4) << 24);
+      unsigned fresh = 0xFFu;
+      int d = 0;
+      for (int i = 0; i < nkb; ++i) {
+        const int st = i % STAGES;
+        if (!mbar_wait(&a_full[st], (i / STAGES) & 1, lim, &s_abort) ||
+            !mbar_wait(&conv_bar[st], (i / STAGES) & 1, lim, &s_abort)) {
+          s_abort = 1;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        issue_any(tbase, sw64_desc(smem_u32(sA + st * a_stage)),
+                  sw64_desc(smem_u32(sB + st * b_stage)), S, idesc, fresh);
+        mma_issued = 1;
+        mma_commit(&empty_bar[st]);
+        if ((i + 1) % KB_PER_DRAIN == 0 && i + 1 < nkb) {
+          mma_commit(&drain_full);
+          if (!mbar_wait(&drain_empty, d & 1, lim, &s_abort)) {
+            s_abort = 1;
+            break;
+          }
+          ++d;
+          fresh = 0xFFu;
+        }
+      }
+      mma_commit(&done_bar);
+    }
+  } else {
+    // Epilogue warps 0-19: convert every K block, drain every 256 K, write.
+    float hi[EPI_COLS], lo[EPI_COLS];
+#pragma unroll
+    for (int c = 0; c < EPI_COLS; ++c) {
+      hi[c] = 0.f;
+      lo[c] = 0.f;
+    }
+    const int col0 = (warp >> 2) * EPI_COLS;
+    const uint32_t tacc = tbase + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)col0;
+    // Conversion task of this thread: column cc of the tile, quarter cq
+    // (4 K entries) of the block's 32 -- 80 x 8 tasks, one per epilogue thread.
+    static_assert(TN * (TK / 4) == NEPI, "one conversion task per epilogue thread");
+    const int cc = tid >> 3, cq = tid & 7;
+    int shift_base = 0;
+    {
+      const int n = nt * TN + cc;
+      shift_base = 8 * S - 1076 - (n < a.N ? scale_of_raw(a.eb_raw[n]) : 0);
+    }
+    bool ok = true;
+    int d = 0;
+    for (int i = 0; i < nkb && ok; ++i) {
+      const int st = i % STAGES;
+      // The FP64 tile is here, and the MMAs of block i - STAGES are done with
+      // the B stage the digits go to.
+      ok = mbar_wait(&c_full[st], (i / STAGES) & 1, lim, &s_abort) &&
+           mbar_wait(&empty_bar[st], ((i / STAGES) & 1) ^ 1, lim, &s_abort);
+      if (!ok) break;
+      convert_quarter<S>(reinterpret_cast<const double*>(sC + st * C64_TILE), sB + st * b_stage,
+                         cc, cq, shift_base);
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      mbar_arrive(&conv_bar[st]);
+      mbar_arrive(&c_empty[st]);
+      if ((i + 1) % KB_PER_DRAIN == 0 && i + 1 < nkb && d < ndrain) {
+        ok = mbar_wait(&drain_full, d & 1, lim, &s_abort);
+        if (!ok) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        drain_tmem(tacc, nacc, hi, lo);
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        mbar_arrive(&drain_empty);
+        ++d;
+      }
+    }
+    if (ok) ok = mbar_wait(&done_bar, 0, lim, &s_abort);
+    if (!ok) {
+      s_abort = 1;
+    } else {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      drain_tmem(tacc, nacc, hi, lo);
+      const int r = mt * TM + (warp & 3) * 32 + lane;
+      if (r < a.M)
+        write_row(a, r, nt * TN + col0, a.C + (long long)r * a.crs + (long long)z * a.zstride, hi,
+                  lo, true);
+    }
+  }
+
+  // Teardown: on abort, wait (bounded) for in-flight copies and MMAs first.
+  __syncthreads();
+  if (s_abort) {
+    if (tid == 0) atomicCAS(a.err, 0, HQ_ERR_BARRIER_TIMEOUT);
+    if (warp == PRODUCER_WARP && lane == 0) {
+      for (int i = a_issued > STAGES ? a_issued - STAGES : 0; i < a_issued; ++i)
+        mbar_wait(&a_full[i % STAGES], (i / STAGES) & 1, lim, nullptr);
+    }
+    if (warp == PRODUCER_WARP && lane == 1) {
+      for (int i = c_issued > STAGES ? c_issued - STAGES : 0; i < c_issued; ++i)
+        mbar_wait(&c_full[i % STAGES], (i / STAGES) & 1, lim, nullptr);
+    }
+    if (warp == MMA_WARP && lane == 0 && mma_issued) mbar_wait(&done_bar, 0, lim, nullptr);
     __syncthreads();
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -1059,6 +1313,7 @@ extern "C" int hq_ozk_gemm(cudaStream_t stream, const hq_device_info* dev, int M
   a.spin_limit = spin_limit;
   a.colexp = nullptr;
   a.row_lo = 0;
+  a.eb_raw = nullptr;
   if (Z > 1) {
     a.C = ws;
     a.crs = 1;
@@ -1086,6 +1341,102 @@ extern "C" int hq_ozk_gemm(cudaStream_t stream, const hq_device_info* dev, int M
       cudaFuncSetAttribute(ozk_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return (int)e;
   ozk_gemm_kernel<<<dim3(MT, NTL, Z), NT, smem, stream>>>(a, tmA, tmB);
+  hq_count_launches(1);
+  if (Z > 1) {
+    long long total = (long long)M * N;
+    int blocks = (int)((total + 255) / 256);
+    if (blocks > dev->num_sms * 8) blocks = dev->num_sms * 8;
+    ozk_sum_slices<<<blocks, 256, 0, stream>>>(M, N, Z, ws, C, crs, ccs, 0);
+    hq_count_launches(1);
+  }
+  return (int)cudaGetLastError();
+}
+
+// W1-style product with an FP64 N-side operand: Y element (n, k) at
+// Y[n * yld + k] (k contiguous), n < N, k < K; raw[n] = row n's largest
+// exponent field.  Mode 0 only (C = sign * A Y^T, split K through ws as in
+// hq_ozk_gemm).  Returns cudaErrorNotSupported when Y's layout does not meet
+// the tensor-map rules (16-byte aligned base and stride), so the caller can
+// split Y instead.
+extern "C" int hq_ozk_gemm_c64(cudaStream_t stream, const hq_device_info* dev, int M, int N,
+                               int K, const void* Atiles, const int* ea, const double* Y,
+                               long long yld, const int* raw, double sign, double* C,
+                               long long crs, long long ccs, double* ws, size_t ws_elems,
+                               int* err, unsigned spin_limit) {
+  if (M <= 0 || N <= 0 || K <= 0) return 0;
+  constexpr int S = 7;
+  if ((reinterpret_cast<uintptr_t>(Y) & 15) != 0 || ((yld * 8) & 15) != 0 || yld < K)
+    return (int)cudaErrorNotSupported;
+  const size_t smem = (size_t)2 * (S * (A_TILE + B_TILE) + C64_TILE) + 1024;
+  if (smem > dev->smem_optin) return (int)cudaErrorNotSupported;
+  const int MT = (M + TM - 1) / TM, NTL = (N + TN - 1) / TN, KB = (K + TK - 1) / TK;
+  int Z = 1;
+  if (ws != nullptr) {
+    const long long tiles = (long long)MT * NTL;
+    const int max_z = (KB + KB_PER_DRAIN - 1) / KB_PER_DRAIN;
+    while (Z < max_z && tiles * Z < 2LL * dev->num_sms && (size_t)(Z + 1) * M * N <= ws_elems)
+      ++Z;
+  }
+  int kb_per_z = (KB + Z - 1) / Z;
+  kb_per_z = (kb_per_z + KB_PER_DRAIN - 1) / KB_PER_DRAIN * KB_PER_DRAIN;
+  Z = (KB + kb_per_z - 1) / kb_per_z;
+  OzkArgs a;
+  a.A = static_cast<const uint8_t*>(Atiles);
+  a.B = nullptr;
+  a.ea = ea;
+  a.eb = nullptr;
+  a.eb_raw = raw;
+  a.M = M;
+  a.N = N;
+  a.S = S;
+  a.KB = KB;
+  a.kb_per_z = kb_per_z;
+  a.mode = 0;
+  a.sign = sign;
+  a.err = err;
+  a.spin_limit = spin_limit;
+  a.colexp = nullptr;
+  a.row_lo = 0;
+  a.stages = 2;
+  if (Z > 1) {
+    a.C = ws;
+    a.crs = 1;
+    a.ccs = M;
+    a.zstride = (long long)M * N;
+  } else {
+    a.C = C;
+    a.crs = crs;
+    a.ccs = ccs;
+    a.zstride = 0;
+  }
+  CUtensorMap tmA, tmC;
+  int rc = make_digit_map(&tmA, Atiles, M, K, S, TM);
+  if (rc) return rc;
+  {
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (encode == nullptr) {
+      void* fn = nullptr;
+      cudaDriverEntryPointQueryResult q;
+      cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
+                                                       cudaEnableDefault, &q);
+      if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || fn == nullptr)
+        return (int)cudaErrorNotSupported;
+      encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }
+    const cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)N};
+    const cuuint64_t strides[1] = {(cuuint64_t)yld * 8};
+    const cuuint32_t box[2] = {(cuuint32_t)TK, (cuuint32_t)TN};
+    const cuuint32_t estr[2] = {1, 1};
+    CUresult r = encode(&tmC, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, const_cast<double*>(Y), dims,
+                        strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return (int)cudaErrorNotSupported;
+  }
+  cudaError_t e = cudaFuncSetAttribute(ozk_gemm_c64_kernel,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return (int)e;
+  ozk_gemm_c64_kernel<<<dim3(MT, NTL, Z), NT, smem, stream>>>(a, tmA, tmC);
   hq_count_launches(1);
   if (Z > 1) {
     long long total = (long long)M * N;
@@ -1129,6 +1480,7 @@ extern "C" int hq_ozk_gemm_short(cudaStream_t stream, const hq_device_info* dev,
   a.zstride = 0;
   a.colexp = mode == 1 ? colexp : nullptr;
   a.row_lo = row_lo;
+  a.eb_raw = nullptr;
   const size_t per_stage = (size_t)S * (A_TILE + B_TILE);
   int stages = MAX_STAGES;
   while (stages > 2 && (size_t)stages * per_stage + 1024 > dev->smem_optin) --stages;

@@ -68,13 +68,14 @@ __global__ void __launch_bounds__(NT) qrp_batched_kernel(BatchArgs a) {
       if (tid == 0 && a.info) a.info[item] = bad ? HQ_ERR_BAD_SHAPE : 0;
       continue;
     }
-    const bool staged = (long long)m * n * 8 <= a.stage_bytes;
+    const int lds = m;
+    const bool staged = (long long)lds * n * 8 <= a.stage_bytes;
     double* X = staged ? sX : Ag;
-    const int ldx = staged ? m : lda;
+    const int ldx = staged ? lds : lda;
     if (staged)
       for (long long e = tid; e < (long long)m * n; e += NT) {
         const int i = (int)(e % m), k = (int)(e / m);
-        sX[e] = Ag[i + (long long)k * lda];
+        sX[i + (long long)k * lds] = Ag[i + (long long)k * lda];
       }
     __syncthreads();
     // Initial norms (warp per column, fixed lane order).
@@ -156,8 +157,7 @@ __global__ void __launch_bounds__(NT) qrp_batched_kernel(BatchArgs a) {
         if (tid == 0) xs[s] = 1.0;  // v_s, restored to beta after the update
         __syncthreads();
       }
-      // w_k = tau * v^T X[s:, k]; X[s:, k] -= v w_k (warp per column), and the
-      // norm downdate of column k by lane 0.
+      // w_k = tau * v^T X[s:, k]; X[s:, k] -= v w_k, a warp per column.
       const double tau = s_tau;
       for (int k = s + 1 + warp; k < n; k += NW) {
         double* xk = X + (long long)k * ldx;
@@ -165,19 +165,34 @@ __global__ void __launch_bounds__(NT) qrp_batched_kernel(BatchArgs a) {
         for (int i = s + lane; i < m; i += 32) w = fma(xs[i], xk[i], w);
         w = hq_warp_sum(w) * tau;
         for (int i = s + lane; i < m; i += 32) xk[i] = fma(-xs[i], w, xk[i]);
-        __syncwarp();
+      }
+      __syncthreads();
+      // LAWN 176 downdate of the partial norms, one thread per column, from
+      // the new entries of row s (a warp per column would repeat its
+      // divisions and square root on 32 lanes of the scarce FP64 pipe);
+      // columns that need their norm recomputed are flagged and recomputed
+      // below, a warp per column (rare).
+      int* sflag = reinterpret_cast<int*>(sw);
+      int any = 0;
+      for (int k = s + 1 + tid; k < n; k += NT) {
         double dk = sd[k];
-        bool recompute = false;
+        int flag = 0;
         if (dk != 0.0) {
-          double t1 = fabs(xk[s]) / dk;
+          double t1 = fabs(X[s + (long long)k * ldx]) / dk;
           t1 = (1.0 + t1) * (1.0 - t1);
           if (0.0 > t1) t1 = 0.0;
           const double ratio = dk / se[k];
           const double t2 = t1 * ratio * ratio;
-          if (t2 <= HQ_TOL3Z) recompute = true;
-          else if (lane == 0) sd[k] = dk * sqrt(t1);
+          if (t2 <= HQ_TOL3Z) flag = 1;
+          else sd[k] = dk * sqrt(t1);
         }
-        if (recompute) {
+        sflag[k] = flag;
+        any |= flag;
+      }
+      if (__syncthreads_or(any)) {
+        for (int k = s + 1 + warp; k < n; k += NW) {
+          if (!sflag[k]) continue;  // uniform across the warp
+          const double* xk = X + (long long)k * ldx;
           double q = 0.0;
           for (int i = s + 1 + lane; i < m; i += 32) q = fma(xk[i], xk[i], q);
           q = hq_warp_sum(q);
@@ -187,15 +202,15 @@ __global__ void __launch_bounds__(NT) qrp_batched_kernel(BatchArgs a) {
             se[k] = nv;
           }
         }
+        __syncthreads();
       }
-      __syncthreads();
       if (tid == 0) xs[s] = s_beta;
       __syncthreads();
     }
     if (staged)
       for (long long e = tid; e < (long long)m * n; e += NT) {
         const int i = (int)(e % m), k = (int)(e / m);
-        Ag[i + (long long)k * lda] = sX[e];
+        Ag[i + (long long)k * lda] = sX[i + (long long)k * lds];
       }
     for (int k = tid; k < n; k += NT) a.jpvt[item][k] = sperm[k] + 1;
     if (tid == 0 && a.info) a.info[item] = 0;

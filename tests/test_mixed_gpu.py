@@ -119,3 +119,25 @@ def test_mixed_dgeqp4_small_path_fixed_columns(mixed, m, n, every):
     assert sorted(jpvt[:nf]) == [i + 1 for i in range(0, n, every)]
     res, orth, _ = oracle.quality(A, Af, jpvt, tau)
     assert res <= 1e-13 and orth <= 1e-12, (res, orth)
+
+
+@pytest.mark.parametrize("m,n,nb", [(2000, 1800, 128), (1500, 1500, 64)])
+def test_trailing_digits_cut_on_the_fly_are_the_split_digits(hq, m, n, nb):
+    """From the second block on, W1 = U'^T C reads C as FP64 and cuts its
+    digits in shared memory (scales from the previous update's column
+    exponents) instead of a separate split pass: the digits are the same, so
+    the factorization is bit-identical to the split path's."""
+    import os
+    A = oracle.gaussian(m, n, m + 2 * n)
+    prev = hq.set_precision(hq.MIXED)
+    try:
+        a = hq.hqrrp(A, nb, 10, 1)
+        os.environ["HQRRP_GB300_SPLIT_TRAILING"] = "1"
+        try:
+            b = hq.hqrrp(A, nb, 10, 1)
+        finally:
+            os.environ.pop("HQRRP_GB300_SPLIT_TRAILING", None)
+    finally:
+        hq.set_precision(prev)
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x, y)
