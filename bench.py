@@ -49,8 +49,10 @@ sys.path.insert(0, ROOT)
 METRIC = "dgeqp4 TFLOP/s at n=16384, mixed vs plain FP64 at equal residual; bwd ms"
 # DRAM bytes per algorithmic flop of the dominant kernels, from ncu captures at
 # m = n = 6144 (committed summaries under profiles/): the split-BF16 products
-# (W1 and the rank-b update) and the FP64 update GEMMs (W1, C -= U W2).
-TENSOR_BYTES_PER_FLOP = (550.2e6 + 556.1e6) / (2 * 2.649e11)
+# -- W1 = U'^T C reading C as FP64 (302.1 MB per 2.43e11 BF16 flops,
+# ozk_gemm_c64_n6144.md) and C -= U'W2 (556.1 MB per 2.649e11, ozk_gemm_n6144.md)
+# -- and the FP64 update GEMMs of the plain path (W1, C -= U W2).
+TENSOR_BYTES_PER_FLOP = (302.1e6 + 556.1e6) / (2.43e11 + 2.649e11)
 FP64_UPDATE_BYTES_PER_FLOP = (314.4e6 + 546.3e6) / (2 * 9.462e9)
 
 
@@ -82,6 +84,8 @@ def parse():
     p.add_argument("--ref-n", type=int, default=16384, help="reference-arm matrix size")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-adjoint", action="store_true", help="skip the bwd_ms measurement")
+    p.add_argument("--single", action="store_true",
+                   help="one untimed factorization of the workload's matrix (for profilers)")
     p.add_argument("--no-extras", action="store_true",
                    help="square workload only: skip the nested tall and batched lines")
     return p.parse_args()
@@ -675,8 +679,8 @@ def roofline_of(H, head, peaks, device):
                     if peaks.get("bf16_tflops_sustained") else "fallback 1.7 PFLOP/s sustained",
                     "launches": n_t, "flops_per_launch": t_fl / n_t,
                     "traffic": TENSOR_BYTES_PER_FLOP * t_fl / n_t,
-                    "traffic_source": "ncu dram__bytes_read+write at 6144^2 scaled by flops "
-                                      "per launch"}
+                    "traffic_source": "ncu dram__bytes_read+write of W1 and C -= U'W2 at "
+                                      "6144^2, scaled by flops per launch"}
     else:
         u_ms, u_fl = H["prof"]["update"]
         peak = fp64_peak_tflops(device)
@@ -750,6 +754,17 @@ def e2e_host(hq, At0, m, n, nb, pp, steps, head, world, dist, device):
         if it > 0:
             ltimes.append(dt)
     lsec = sum(ltimes) / len(ltimes)
+    # One more (untimed) dgeqp4 under the phase profiler: where nb = 64 loses
+    # against nb = 128.
+    hA.copy_(host0)
+    hjp.zero_()
+    hq.profile_enable(True)
+    hq.profile_read()
+    L.dgeqp4(C.byref(mi), C.byref(ni), C.cast(hA.data_ptr(), dp), C.byref(ldi),
+             C.cast(hjp.data_ptr(), ip), C.cast(htau.data_ptr(), dp), work,
+             C.byref(lwork), C.byref(info))
+    dprof = phase_table(hq.profile_read())
+    hq.profile_enable(False)
     del hA
     # pageable host memory (numpy)
     pA0 = host0.numpy().copy()
@@ -777,7 +792,8 @@ def e2e_host(hq, At0, m, n, nb, pp, steps, head, world, dist, device):
             "ms_per_step": sec * 1e3, "precision": head,
             "api": "NoFLA_HQRRP_WY_blk_var4(nb=%d, pp=%d), host page-locked buffers" % (nb, pp),
             "dgeqp4": {"value": fl / lsec / 1e12, "unit": "TFLOP/s", "ms_per_step": lsec * 1e3,
-                       "api": "dgeqp4 (HQRRP nb=64, pp=10 inside), host page-locked buffers"},
+                       "api": "dgeqp4 (HQRRP nb=64, pp=10 inside), host page-locked buffers",
+                       "phases_ms": dprof[0], "phases_tflops": dprof[1]},
             "pageable": {"value": fl / psec / 1e12, "unit": "TFLOP/s", "ms_per_step": psec * 1e3,
                          "api": "NoFLA_HQRRP_WY_blk_var4(nb=%d, pp=%d), host pageable (numpy) "
                                 "buffers" % (nb, pp)}}
@@ -846,6 +862,40 @@ def run_factorization(hq, args, name, device, dist, rank, world, local, steps, w
     return line, At0
 
 
+def run_single(hq, args, device):
+    """One factorization of the square (or tall) workload's matrix, untimed:
+    the command the ncu launch lists and captures run."""
+    import torch
+    if args.workload == "batched":
+        shapes = batched_shapes(args.batch, args.seed)
+        flat, offs = make_batched_gpu(shapes, args.seed, device)
+        mats = [flat[offs[i]:offs[i + 1]].view(n, m) for i, (m, n) in enumerate(shapes)]
+        bq = hq.BatchedQRP(shapes, autotune=False)
+        bq.cfg = 3  # 256 threads, 96 KB staging, 2 CTAs per SM
+        torch.cuda.synchronize()
+        _, _, info = bq.run(mats)
+        torch.cuda.synchronize()
+        if int(info.abs().sum()) != 0:
+            raise RuntimeError("batched QR reported errors")
+        print("factored %d matrices" % len(shapes))
+        return
+    if args.workload == "tall":
+        n = args.n or 8192
+        m = args.m or 4 * n
+        sigma = spectrum_tall(min(m, n))
+    else:
+        n = m = args.n or 16384
+        sigma = spectrum(n)
+    At = make_matrix_gpu(m, n, sigma, args.seed, device)
+    jp = torch.arange(1, n + 1, dtype=torch.int32, device=device)
+    tau = torch.zeros(min(m, n), dtype=torch.float64, device=device)
+    hq.set_precision(hq.PLAIN if args.precision == "plain" else hq.MIXED)
+    torch.cuda.synchronize()
+    hq.hqrrp_device(At, jp, tau, args.nb, args.pp, 1)
+    torch.cuda.synchronize()
+    print("factored %d x %d (%s)" % (m, n, "plain" if args.precision == "plain" else "mixed"))
+
+
 def sub_line(d, keep=("value", "unit", "ms_per_step", "steps", "warmup", "config", "quality",
                       "roofline", "e2e", "plain", "mixed_over_plain", "gpu_launches", "clocks",
                       "matrices_per_s", "cpu_baseline")):
@@ -873,6 +923,9 @@ def main():
     device = torch.device("cuda", local)
     torch.cuda.set_device(device)
 
+    if args.single:
+        run_single(hq, args, device)
+        return
     if args.workload == "batched":
         line = run_batched(hq, args, device, dist, rank, world, local, args.steps, args.warmup)
         if line is not None:

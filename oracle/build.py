@@ -8,8 +8,10 @@ Two shared libraries come out of this recipe:
 * ``oracle/_ref/libhqrrp_ref.so`` -- the unmodified reference source
   ``lapack_compatible_sources/NoFLA_HQRRP_WY_blk_var4.c`` compiled through
   ``ref_wrap.c`` and linked to scipy's bundled OpenBLAS.  Built only where the
-  reference tree is present (``HQRRP_REFERENCE_DIR`` or the default mount);
-  elsewhere the restatement alone is the oracle.
+  reference tree is found: the ``reference`` argument, else the
+  ``HQRRP_REFERENCE_DIR`` environment variable, else DEFAULT_REFERENCE (where
+  this recipe's build container mounts it); elsewhere the restatement alone
+  is the oracle.
 
 Nothing here is imported by the product package.
 """
@@ -23,6 +25,8 @@ LIB_DIR = os.path.join(HERE, "_lib")
 REF_DIR = os.path.join(HERE, "_ref")
 ORACLE_SO = os.path.join(LIB_DIR, "libhqrrp_oracle.so")
 REF_SO = os.path.join(REF_DIR, "libhqrrp_ref.so")
+# Where the build container mounts the reference project; the argument and
+# HQRRP_REFERENCE_DIR take precedence.
 DEFAULT_REFERENCE = "/root/reference"
 
 # LAPACK/BLAS symbols the reference calls; each is mapped onto scipy_<name>_.
@@ -65,15 +69,16 @@ def build_oracle(force=False):
     return ORACLE_SO
 
 
-def reference_dir():
-    d = os.environ.get("HQRRP_REFERENCE_DIR", DEFAULT_REFERENCE)
+def reference_dir(reference=None):
+    """The reference project's root, or None where its source is absent."""
+    d = reference or os.environ.get("HQRRP_REFERENCE_DIR") or DEFAULT_REFERENCE
     src = os.path.join(d, "lapack_compatible_sources", "NoFLA_HQRRP_WY_blk_var4.c")
     return d if os.path.exists(src) else None
 
 
-def build_reference(force=False):
+def build_reference(force=False, reference=None):
     """Compile the unmodified reference; returns the .so path or None."""
-    d = reference_dir()
+    d = reference_dir(reference)
     blas = find_openblas()
     if d is None or blas is None:
         return REF_SO if os.path.exists(REF_SO) else None
@@ -87,10 +92,10 @@ def build_reference(force=False):
     return REF_SO
 
 
-def build(force=False):
+def build(force=False, reference=None):
     out = {"oracle": build_oracle(force)}
     try:
-        out["reference"] = build_reference(force)
+        out["reference"] = build_reference(force, reference)
     except RuntimeError as exc:  # the reference is optional
         print(exc, file=sys.stderr)
         out["reference"] = None
@@ -98,4 +103,5 @@ def build(force=False):
 
 
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv))
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    print(build(force="--force" in sys.argv, reference=args[0] if args else None))
