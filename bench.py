@@ -765,6 +765,26 @@ def e2e_host(hq, At0, m, n, nb, pp, steps, head, world, dist, device):
              C.byref(lwork), C.byref(info))
     dprof = phase_table(hq.profile_read())
     hq.profile_enable(False)
+    # dgeqp4 with the GPU's block size for its HQRRP call (128 instead of the
+    # reference's CPU-chosen 64; hqrrp_gb300_set_dgeqp4_block).
+    prev_nb = hq.set_dgeqp4_block(128)
+    qtimes = []
+    try:
+        for it in range(1 + steps):
+            hA.copy_(host0)
+            hjp.zero_()
+            t0 = time.perf_counter()
+            L.dgeqp4(C.byref(mi), C.byref(ni), C.cast(hA.data_ptr(), dp), C.byref(ldi),
+                     C.cast(hjp.data_ptr(), ip), C.cast(htau.data_ptr(), dp), work,
+                     C.byref(lwork), C.byref(info))
+            dt = time.perf_counter() - t0
+            if info.value != 0:
+                raise RuntimeError("dgeqp4 failed: info %d %s" % (info.value, hq.last_error()))
+            if it > 0:
+                qtimes.append(dt)
+    finally:
+        hq.set_dgeqp4_block(prev_nb)
+    qsec = sum(qtimes) / len(qtimes)
     del hA
     # pageable host memory (numpy)
     pA0 = host0.numpy().copy()
@@ -782,9 +802,9 @@ def e2e_host(hq, At0, m, n, nb, pp, steps, head, world, dist, device):
     psec = sum(ptimes) / len(ptimes)
     del pA, pA0
     if dist:
-        t = torch.tensor([sec, lsec, psec], dtype=torch.float64, device=device)
+        t = torch.tensor([sec, lsec, psec, qsec], dtype=torch.float64, device=device)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        sec, lsec, psec = float(t[0]), float(t[1]), float(t[2])
+        sec, lsec, psec, qsec = float(t[0]), float(t[1]), float(t[2]), float(t[3])
     fl = world * flops_qr(m, n)
     return {"value": fl / sec / 1e12, "unit": "TFLOP/s",
             "h2d_bytes_per_step": 8 * m * n + 4 * n,
@@ -794,6 +814,10 @@ def e2e_host(hq, At0, m, n, nb, pp, steps, head, world, dist, device):
             "dgeqp4": {"value": fl / lsec / 1e12, "unit": "TFLOP/s", "ms_per_step": lsec * 1e3,
                        "api": "dgeqp4 (HQRRP nb=64, pp=10 inside), host page-locked buffers",
                        "phases_ms": dprof[0], "phases_tflops": dprof[1]},
+            "dgeqp4_block128": {"value": fl / qsec / 1e12, "unit": "TFLOP/s",
+                                "ms_per_step": qsec * 1e3,
+                                "api": "dgeqp4 after hqrrp_gb300_set_dgeqp4_block(128), host "
+                                       "page-locked buffers"},
             "pageable": {"value": fl / psec / 1e12, "unit": "TFLOP/s", "ms_per_step": psec * 1e3,
                          "api": "NoFLA_HQRRP_WY_blk_var4(nb=%d, pp=%d), host pageable (numpy) "
                                 "buffers" % (nb, pp)}}

@@ -66,6 +66,8 @@ def load():
     L.NoFLA_HQRRP_WY_blk_var4.restype = C.c_int
     L.hqrrp_gb300_set_precision.argtypes = [C.c_int]
     L.hqrrp_gb300_set_precision.restype = C.c_int
+    L.hqrrp_gb300_set_dgeqp4_block.argtypes = [C.c_int]
+    L.hqrrp_gb300_set_dgeqp4_block.restype = C.c_int
     L.hqrrp_gb300_set_seed.argtypes = [C.c_ulonglong]
     L.hqrrp_gb300_set_seed.restype = None
     L.hqrrp_gb300_set_spin_limit.argtypes = [C.c_uint]
@@ -146,6 +148,15 @@ def last_error():
 
 def set_precision(mode):
     return load().hqrrp_gb300_set_precision(int(mode))
+
+
+def set_dgeqp4_block(nb):
+    """Block size of dgeqp4's HQRRP call (default 64, the reference's);
+    returns the previous value."""
+    prev = load().hqrrp_gb300_set_dgeqp4_block(int(nb))
+    if prev < 0:
+        raise ValueError("dgeqp4 block size must be in 1..246")
+    return prev
 
 
 def set_seed(seed):

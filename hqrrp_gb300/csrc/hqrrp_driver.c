@@ -37,6 +37,7 @@ enum {
 
 #define DGEQP4_SMALL_DGEQP3 1000 /* ...var4.c:58 */
 #define DGEQP4_NB 64 /* HQRRP block size and oversampling dgeqp4 uses (...var4.c:264) */
+static int g_dgeqp4_nb = DGEQP4_NB; /* hqrrp_gb300_set_dgeqp4_block */
 #define DGEQP4_PP 10
 #define LAPACK_NB_DGEQRF 32 /* ILAENV(1, 'DGEQRF') of reference LAPACK */
 #define LAPACK_NX_DGEQRF 128 /* ILAENV(3, 'DGEQRF'): blocked-code crossover */
@@ -97,6 +98,13 @@ HQ_API int hqrrp_gb300_set_precision(int mode) {
 }
 
 HQ_API void hqrrp_gb300_set_seed(unsigned long long seed) { g_seed = seed; }
+
+HQ_API int hqrrp_gb300_set_dgeqp4_block(int nb) {
+  if (nb < 1 || nb + DGEQP4_PP > HQ_MAX_MY) return -1;
+  const int prev = g_dgeqp4_nb;
+  g_dgeqp4_nb = nb;
+  return prev;
+}
 
 HQ_API void hqrrp_gb300_set_spin_limit(unsigned limit) { g_spin_limit = limit; }
 
@@ -182,6 +190,7 @@ typedef struct {
   prof_rec* prof; /* non-NULL while profiling */
   int mixed;      /* split-BF16 tensor-core block updates */
   int ut;         /* UT-transform reflector convention in the panels */
+  int dq_nb;      /* the HQRRP block size dgeqp4 uses in this call */
   void *ozA, *ozB; /* digit tiles of the two operands of a mixed product */
   int *ozea, *ozeb;
   /* Mixed mode: per global column, the largest FP64 exponent field of the
@@ -1115,7 +1124,7 @@ static int core_dgeqp4(hq_ws* w, int m, int n, double* dA, int ldda, int* hjp, i
       CK(hq_permute_cols(w->st, nf, dA + (size_t)nf * ldda, ldda, nt, w->perm, w->tmp,
                          djp + nf, w->label_tmp));
     } else {
-      int rc = core_hqrrp(w, mt, nt, At, ldda, w->labels, dtau + nf, DGEQP4_NB, DGEQP4_PP, 1, dG,
+      int rc = core_hqrrp(w, mt, nt, At, ldda, w->labels, dtau + nf, w->dq_nb, DGEQP4_PP, 1, dG,
                           lddg, g_seed);
       if (rc) return rc;
       double* t2 = w->tmp;
@@ -1146,7 +1155,7 @@ static int dgeqp4_ws(hq_ws* w, int m, int n) {
     int rc = ws_setup(w, m, n, 0, 0, imax(FIXED_BLOCK, imin(n, HQ_MAX_PANEL)));
     return rc;
   }
-  return ws_setup(w, m, n, DGEQP4_NB, DGEQP4_PP, FIXED_BLOCK);
+  return ws_setup(w, m, n, w->dq_nb, DGEQP4_PP, imax(FIXED_BLOCK, w->dq_nb));
 }
 
 static void xerbla_dgeqp3(int arg) {
@@ -1191,6 +1200,8 @@ static void dgeqp4_host(int* m, int* n, double* A, int* lda, int* jpvt, double* 
     *info = 1000 + rc;
     return;
   }
+  /* With the reference's own sketch (74 rows), the reference's block size. */
+  w.dq_nb = G ? DGEQP4_NB : g_dgeqp4_nb;
   int* hjp = malloc(sizeof(int) * (size_t)N);
   rc = hjp ? dgeqp4_ws(&w, M, N) : HQ_E_NOMEM;
   double* dA = rc ? NULL : ws_alloc(&w, sizeof(double) * (size_t)ldda * N);
@@ -1249,6 +1260,7 @@ HQ_API int hqrrp_gb300_dgeqp4_device(int m, int n, double* dA, int ldda, int* d_
   hq_ws w;
   int rc = ws_begin(&w, (cudaStream_t)stream, 1);
   if (rc) return 1000 + rc;
+  w.dq_nb = g_dgeqp4_nb;
   int* hjp = malloc(sizeof(int) * (size_t)n);
   rc = hjp ? dgeqp4_ws(&w, m, n) : HQ_E_NOMEM;
   cudaStream_t st = w.st;

@@ -109,3 +109,14 @@ def test_no_gpu_error_codes(hq):
                                    tau.ctypes.data_as(dp), 8, 2, 1)
     assert rc == 1 and hq.last_error()
     np.testing.assert_array_equal(A, np.eye(40))
+
+
+def test_dgeqp4_block_setter(hq):
+    """Host-side state only: the previous value comes back, invalid sizes are
+    refused and leave it unchanged."""
+    assert hq.set_dgeqp4_block(128) == 64
+    with pytest.raises(ValueError):
+        hq.set_dgeqp4_block(0)
+    with pytest.raises(ValueError):
+        hq.set_dgeqp4_block(247)
+    assert hq.set_dgeqp4_block(64) == 128

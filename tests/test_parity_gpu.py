@@ -317,3 +317,28 @@ def test_dgeqp4_rows_above_follow_hqrrp_bit_exact(hq, oracle_lib):
     np.testing.assert_array_equal(Ag[:nf, nf:], A[:nf, jg[nf:] - 1])
     np.testing.assert_array_equal(Ao[:nf, nf:], A[:nf, jo[nf:] - 1])
     assert_parity((Ag, jg, tg), (Ao, jo, to))
+
+
+def test_dgeqp4_gpu_block_size(hq, oracle_lib):
+    """dgeqp4 with HQRRP block 128 (hqrrp_gb300_set_dgeqp4_block): a different
+    block structure, so its own pivots, but the same quality, fixed columns
+    still first, and an explicit reference sketch still gets the reference's
+    block size 64 (parity with the oracle unchanged)."""
+    m, n = 1500, 1400
+    A = oracle.gaussian(m, n, 47)
+    jp = _fixed_marks(n, 11)
+    prev = hq.set_dgeqp4_block(128)
+    try:
+        Af, jpv, tau, info, _ = hq.dgeqp4(A, jp)
+        G = oracle_lib.sketch(74, m - _nfix(jp, m))
+        got = hq.dgeqp4(A, jp, G=G)
+    finally:
+        hq.set_dgeqp4_block(prev)
+    assert info == 0
+    nf = _nfix(jp, m)
+    assert sorted(jpv[:nf]) == [i + 1 for i in range(0, n, 11)]
+    res, orth, _ = oracle.quality(A, Af, jpv, tau)
+    assert res <= 1e-14 and orth <= 1e-13, (res, orth)
+    Ao, jo, to, io, _ = oracle_lib.dgeqp4(A, jp)
+    assert got[3] == io == 0
+    assert_parity(got[:3], (Ao, jo, to))
