@@ -498,15 +498,31 @@ __device__ __forceinline__ double f32_scaled(float f, int ek, unsigned neg) {
 // Epilogue thread's share of a tile: TMEM lanes of its quadrant (one output
 // row each), EPI_COLS columns starting at col0.  Adds the nacc accumulators
 // of those columns into the float-float running sums.
+// 16 consecutive TMEM columns of this warp's 32 lanes (one load, one wait).
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+      "%14,%15}, [%16];\n"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+// One 16-column TMEM load per accumulator (EPI_COLS = 16): half the
+// load-and-wait round trips of 8-column loads, on the path the MMAs wait for.
 __device__ __forceinline__ void drain_tmem(uint32_t tacc, int nacc, float* hi, float* lo) {
+  static_assert(EPI_COLS == 16, "one 16-column load per accumulator");
+  for (int q = 0; q < nacc; ++q) {
+    float v[16];
+    tmem_ld16(tacc + (uint32_t)(q * TN), v);
 #pragma unroll
-  for (int c8 = 0; c8 < EPI_COLS; c8 += 8) {
-    for (int q = 0; q < nacc; ++q) {
-      float v[8];
-      tmem_ld8(tacc + (uint32_t)(q * TN + c8), v);
-#pragma unroll
-      for (int j = 0; j < 8; ++j) ff_add(hi[c8 + j], lo[c8 + j], v[j]);
-    }
+    for (int j = 0; j < 16; ++j) ff_add(hi[j], lo[j], v[j]);
   }
 }
 
