@@ -93,6 +93,8 @@ def load():
     L.hqrrp_gb300_launch_count.restype = C.c_ulonglong
     L.hqrrp_gb300_pool_alloc_count.argtypes = []
     L.hqrrp_gb300_pool_alloc_count.restype = C.c_ulonglong
+    L.hqrrp_gb300_gram_panel_counts.argtypes = [C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.hqrrp_gb300_gram_panel_counts.restype = C.c_int
     L.hqrrp_gb300_ozaki_dgemm.argtypes = [C.c_char, C.c_char, C.c_int, C.c_int, C.c_int,
                                           C.c_double, C.c_void_p, C.c_int, C.c_void_p, C.c_int,
                                           C.c_double, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
@@ -191,6 +193,17 @@ def profile_counts():
 
 def launch_count():
     return int(load().hqrrp_gb300_launch_count())
+
+
+def gram_panel_counts():
+    """(committed, fallback): the mixed path's Gram panels of the last call
+    that ran any, committed and passed on to the column-by-column panel."""
+    L = load()
+    a, b = C.c_int(0), C.c_int(0)
+    rc = L.hqrrp_gb300_gram_panel_counts(C.byref(a), C.byref(b))
+    if rc != 0:
+        raise HQRRPError("gram_panel_counts failed (%d): %s" % (rc, last_error()))
+    return a.value, b.value
 
 
 def pool_alloc_count():

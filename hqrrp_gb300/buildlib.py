@@ -21,7 +21,8 @@ LIB = os.path.join(HERE, "libhqrrp_gb300.so")
 INCLUDE = os.path.join(ROOT, "include")
 
 CUDA_SOURCES = ["gemm_f64.cu", "sketch.cu", "qrp_skinny.cu", "qrp_panel.cu", "permute.cu",
-                "qrp_noalloc.cu", "qrp_wide.cu", "ozaki.cu", "qrp_batched.cu", "adjoint.cu"]
+                "qrp_noalloc.cu", "qrp_wide.cu", "qrp_gram.cu", "ozaki.cu", "qrp_batched.cu",
+                "adjoint.cu"]
 C_SOURCES = ["hqrrp_driver.c"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -65,7 +65,44 @@ int hq_panel_qrp(cudaStream_t stream, const hq_device_info* dev, int mp, int nc,
                  int* perm, double* part, size_t part_elems, double* rowbuf, unsigned* bar,
                  int* err, unsigned spin_limit,
                  int sqnorm, int ut);
+/* The same, skipped (every CTA returns at once) when *gram_stat == 0: the
+ * mixed path's Gram panel (qrp_gram.cu) already factored this panel. */
+int hq_panel_qrp_fallback(cudaStream_t stream, const hq_device_info* dev, int mp, int nc,
+                          int pivoting, double* P, int ldp, double* tau, double* U, int ldu,
+                          int* perm, double* part, size_t part_elems, double* rowbuf,
+                          unsigned* bar, int* err, unsigned spin_limit, int sqnorm, int ut,
+                          const int* gram_stat);
 size_t hq_panel_part_elems(const hq_device_info* dev, int nc);
+
+/* ---- Gram panel (mixed path): the b x b kernels of qrp_gram.cu -----------
+ * All matrices column-major, b <= HQ_GRAM_MAX.  Status bits go to *stat. */
+#define HQ_GRAM_MAX 128
+/* Pass 1: pivoted Cholesky of G (lower triangle read) scaled to unit
+ * diagonal, in FP32: perm[k] = source column of position k, R (FP64, upper)
+ * with R^T R ~ P^T G P; *stat := 0, or bit with R = I, perm = identity. */
+int hq_gram_pchol32(cudaStream_t stream, int n, const double* G, int ldg, double* R, int ldr,
+                    int* perm, int* stat, int bit);
+/* FP64 on a cluster of eight CTAs.  mode 0: Cholesky of the symmetric A
+ * (lower triangle read), F := R upper.  mode 1: LU without pivoting of A - D
+ * (Householder reconstruction), F := L strictly below the diagonal and U on
+ * and above, dsgn := D, tau := -D U_kk.  A bad pivot sets bit in *stat and
+ * gives identity factors. */
+int hq_cluster_fact(cudaStream_t stream, int n, int mode, const double* A, int lda, double* F,
+                    int ldf, double* dsgn, double* tau, int* stat, int bit);
+/* mode 0: X = A^{-1}; mode 1: X = diag(rs) A B (rs may be NULL); A, B upper. */
+int hq_tri(cudaStream_t stream, int n, int mode, const double* A, int lda, const double* B,
+           int ldb, const double* rs, double* X, int ldx);
+/* Two independent such jobs in one launch (mode1 = -1: the first only). */
+int hq_tri2(cudaStream_t stream, int n, int mode0, const double* A0, int lda0, const double* B0,
+            int ldb0, const double* rs0, double* X0, int ldx0, int mode1, const double* A1,
+            int lda1, const double* B1, int ldb1, const double* rs1, double* X1, int ldx1);
+/* When *stat == 0: the panel P (mp x n) := R (RH's upper triangle) and the
+ * Householder vectors (LU's strict lower part; U's rows >= n), U's top rows
+ * := explicit unit-lower V1, tau := tau_in, perm := identity.  count (may be
+ * NULL): count[0] += 1 if committed, count[1] += 1 if not. */
+int hq_gram_commit(cudaStream_t stream, int mp, int n, double* P, int ldp, double* U, int ldu,
+                   const double* RH, int ldr, const double* LU, int ldlu, const double* tau_in,
+                   double* tau, int* perm, const int* stat, int* count);
 /* Exchange area of the panel kernel for `ctas` CTAs and nc columns, in
  * doubles: [2][ps][ctas] FP64 partials (initial and recomputed norms), then
  * [3][ps][HQ_PANEL_FX_CS] 64-bit words of fixed-point stage sums (four used

@@ -215,6 +215,13 @@ typedef struct {
   int drain_lda, drain_ldda, drain_rows, drain_done;
   cudaStream_t cp;
   cudaEvent_t ev_cp;
+  /* Mixed mode: the Gram panel (qrp_gram.cu).  gQ holds Q1, then Q (mp x b,
+   * ldu); the b x b matrices (ld HQ_GRAM_MAX): G and G2, R1, R2, an inverse,
+   * the LU of Q11 - D, and R; gstat is the panel's status word. */
+  int gram;
+  double *gQ, *gG, *gR1, *gR2, *gRi, *gLU, *gRH, *gsgn, *gtau;
+  int *gperm, *gstat, *gcount; /* gcount: panels committed, panels passed on */
+  int ph_override; /* >= 0: charge split-product intervals to this phase */
 } hq_ws;
 
 /* Close the interval since the previous mark and charge it to `phase`. */
@@ -280,6 +287,20 @@ HQ_API unsigned long long hqrrp_gb300_launch_count(void) { return hq_launches();
  * started. */
 static unsigned long long g_pool_allocs = 0;
 
+/* The Gram panel's counts of the last call that ran it (page-locked, written
+ * by a copy on the call's stream when its workspace is released). */
+static int* g_gram_counts = NULL;
+
+HQ_API int hqrrp_gb300_gram_panel_counts(int* committed, int* fallback) {
+  if (cudaDeviceSynchronize() != cudaSuccess) {
+    set_err("cudaDeviceSynchronize failed: %s", cudaGetErrorString(cudaGetLastError()));
+    return HQ_E_CUDA;
+  }
+  *committed = g_gram_counts ? g_gram_counts[0] : 0;
+  *fallback = g_gram_counts ? g_gram_counts[1] : 0;
+  return HQ_OK;
+}
+
 HQ_API unsigned long long hqrrp_gb300_pool_alloc_count(void) {
   return __atomic_load_n(&g_pool_allocs, __ATOMIC_RELAXED);
 }
@@ -318,6 +339,15 @@ static void* ws_alloc(hq_ws* w, size_t bytes) {
 }
 
 static void ws_release(hq_ws* w) {
+  if (w->gcount) {
+    if (!g_gram_counts && cudaHostAlloc((void**)&g_gram_counts, 2 * sizeof(int), 0) != cudaSuccess) {
+      cudaGetLastError();
+      g_gram_counts = NULL;
+    }
+    if (g_gram_counts)
+      cudaMemcpyAsync(g_gram_counts, w->gcount, 2 * sizeof(int), cudaMemcpyDeviceToHost, w->st);
+    w->gcount = NULL;
+  }
   if (w->cp) {
     /* The copy stream reads the matrix: it finishes before anything is freed. */
     cudaEventRecord(w->ev_cp, w->cp);
@@ -431,9 +461,33 @@ static int ws_setup(hq_ws* w, int m, int n, int nb, int pp, int pw) {
     w->ozU = ws_alloc(w, hq_ozk_tile_bytes(m, kmax, S, 0));
     w->ozUTe = ws_alloc(w, sizeof(int) * (size_t)(kmax + 128));
     w->ozUe = ws_alloc(w, sizeof(int) * (size_t)(imax(m, 1) + 128));
+    /* The Gram panel, unless HQRRP_GB300_GRAM_PANEL=0 (the cooperative
+     * column-by-column panel only) or the UT convention is asked for. */
+    const char* ge = getenv("HQRRP_GB300_GRAM_PANEL");
+    w->gram = !(ge && ge[0] == '0');
+    if (w->gram) {
+      const size_t sq = (size_t)HQ_GRAM_MAX * HQ_GRAM_MAX;
+      w->gQ = ws_alloc(w, sizeof(double) * (size_t)w->ldu * imin(kmax, HQ_GRAM_MAX));
+      double* sm = ws_alloc(w, sizeof(double) * (6 * sq + 2 * HQ_GRAM_MAX));
+      w->gperm = ws_alloc(w, sizeof(int) * (HQ_GRAM_MAX + 3));
+      if (sm && w->gperm) {
+        w->gG = sm;
+        w->gR1 = sm + sq;
+        w->gR2 = sm + 2 * sq;
+        w->gRi = sm + 3 * sq;
+        w->gLU = sm + 4 * sq;
+        w->gRH = sm + 5 * sq;
+        w->gsgn = sm + 6 * sq;
+        w->gtau = w->gsgn + HQ_GRAM_MAX;
+        w->gstat = w->gperm + HQ_GRAM_MAX;
+        w->gcount = w->gstat + 1;
+      }
+    }
   }
+  w->ph_override = -1;
   if (w->failed) return HQ_E_NOMEM;
   CK(cudaMemsetAsync(w->err, 0, sizeof(int) * 2, w->st));
+  if (w->gcount) CK(cudaMemsetAsync(w->gcount, 0, sizeof(int) * 2, w->st));
   prof_start(w);
   return HQ_OK;
 }
@@ -472,20 +526,25 @@ static int ozk_product_x(hq_ws* w, int S, int M, int N, int K, const double* X, 
    * products. */
   const void* at = xt ? xt : w->ozA;
   const int* ae = xt ? xe : w->ozea;
+  const int ovr = w->ph_override;
   if (!xt) CK(hq_ozk_split(w->st, X, xrs, xks, M, K, S, 0, w->ozA, w->ozea));
   if (y_raw)
     CK(hq_ozk_split_raw(w->st, Y, yrs, yks, N, K, S, short_k ? 2 : 1, w->ozB, w->ozeb, y_raw));
   else
     CK(hq_ozk_split(w->st, Y, yrs, yks, N, K, S, short_k ? 2 : 1, w->ozB, w->ozeb));
-  prof_mark(w, PH_SPLIT, 0.0);
+  prof_mark(w, ovr >= 0 ? ovr : PH_SPLIT, 0.0);
   if (short_k)
     CK(hq_ozk_gemm_short(w->st, &w->ds->dev, M, N, K, S, at, ae, w->ozB, w->ozeb, mode, sign, Cm,
                          crs, ccs, c_exp, c_row_lo, w->err, spin_limit()));
   else
     CK(hq_ozk_gemm(w->st, &w->ds->dev, M, N, K, S, at, ae, w->ozB, w->ozeb, mode, sign, Cm, crs,
                    ccs, w->ws, w->ws_elems, w->err, spin_limit()));
-  /* flops charged: the BF16 tensor work, S(S+1)/2 digit products */
-  prof_mark(w, PH_TENSOR, (double)S * (S + 1) * M * N * (double)K);
+  /* flops charged: the BF16 tensor work, S(S+1)/2 digit products (none
+   * when the interval belongs to another phase, which charges its own) */
+  if (ovr >= 0)
+    prof_mark(w, ovr, 0.0);
+  else
+    prof_mark(w, PH_TENSOR, (double)S * (S + 1) * M * N * (double)K);
   return HQ_OK;
 }
 
@@ -576,6 +635,57 @@ static int drain_finish(hq_ws* w, double* host, int lda, const double* dev, int 
  * ~2^-47 over long dot products.  The identity's share is exact algebra added
  * in FP64: U^T U = U'^T U' + L + L^T + I, U^T C = U'^T C + C[0:b, :],
  * U W2 = U' W2 + [W2; 0]. */
+/* Mixed mode: factor block j's panel [j, j + b) x [j, m) with the Gram panel
+ * (qrp_gram.cu): Gram and CholeskyQR2 products on the tensor cores, the
+ * b x b factorizations in small kernels (the pivoted first pass in FP32 on
+ * one SM, the FP64 Cholesky and LU on a cluster), Householder
+ * reconstruction.  The panel's
+ * pivots are applied to all m rows of its columns and to jpvt before the
+ * products; the factorization is written by the commit kernel only when
+ * every step succeeded (*gstat == 0), and otherwise the cooperative panel
+ * that follows on the stream factors the (permuted) panel itself. */
+static int gram_panel(hq_ws* w, int m, int j, int b, int piv, double* AR, int ldda, int* jp,
+                      double* tau) {
+  const int mp = m - j, L = HQ_GRAM_MAX, S = OZK_SLICES;
+  double* ABR = AR + j;
+  int rc;
+  w->ph_override = PH_PANEL;
+  /* G = Ap^T Ap; R1, P (pivoted Cholesky); R1^{-1} */
+  rc = ozk_product(w, S, b, b, mp, ABR, ldda, 1, ABR, ldda, 1, 0, 1.0, w->gG, 1, L);
+  if (rc) return rc;
+  if (piv) {
+    CK(hq_gram_pchol32(w->st, b, w->gG, L, w->gR1, L, w->gperm, w->gstat, 1));
+  } else {
+    CK(hq_fill_iota(w->st, w->gperm, b, 0));
+    CK(cudaMemsetAsync(w->gstat, 0, sizeof(int), w->st));
+    CK(hq_cluster_fact(w->st, b, 0, w->gG, L, w->gR1, L, NULL, NULL, w->gstat, 1));
+  }
+  CK(hq_tri(w->st, b, 0, w->gR1, L, NULL, 0, NULL, w->gRi, L));
+  CK(hq_permute_cols(w->st, m, AR, ldda, b, w->gperm, w->tmp, jp, w->label_tmp));
+  /* Q1 = Ap P R1^{-1}; G2 = Q1^T Q1; R2; Q = Q1 R2^{-1} (in place) */
+  rc = ozk_product(w, S, mp, b, b, ABR, 1, ldda, w->gRi, L, 1, 0, 1.0, w->gQ, 1, w->ldu);
+  if (!rc) rc = ozk_product(w, S, b, b, mp, w->gQ, w->ldu, 1, w->gQ, w->ldu, 1, 0, 1.0, w->gG, 1, L);
+  if (rc) return rc;
+  CK(hq_cluster_fact(w->st, b, 0, w->gG, L, w->gR2, L, NULL, NULL, w->gstat, 2));
+  CK(hq_tri(w->st, b, 0, w->gR2, L, NULL, 0, NULL, w->gRi, L));
+  rc = ozk_product(w, S, mp, b, b, w->gQ, 1, w->ldu, w->gRi, L, 1, 0, 1.0, w->gQ, 1, w->ldu);
+  if (rc) return rc;
+  /* Q11 - D = L U; R = D R2 R1; V2 = Q2 U^{-1} (into U's rows >= b) */
+  CK(hq_cluster_fact(w->st, b, 1, w->gQ, w->ldu, w->gLU, L, w->gsgn, w->gtau, w->gstat, 4));
+  /* R_H = D R2 R1 and U^{-1}, one launch */
+  CK(hq_tri2(w->st, b, 1, w->gR2, L, w->gR1, L, w->gsgn, w->gRH, L, mp > b ? 0 : -1, w->gLU, L,
+             NULL, 0, NULL, w->gRi, L));
+  if (mp > b) {
+    rc = ozk_product(w, S, mp - b, b, b, w->gQ + b, 1, w->ldu, w->gRi, L, 1, 0, 1.0, w->U + b, 1,
+                     w->ldu);
+    if (rc) return rc;
+  }
+  CK(hq_gram_commit(w->st, mp, b, ABR, ldda, w->U, w->ldu, w->gRH, L, w->gLU, L, w->gtau, tau,
+                    w->perm, w->gstat, w->gcount));
+  w->ph_override = -1;
+  return HQ_OK;
+}
+
 static int block_reflector(hq_ws* w, int mp, int b, const double* tau, double* Cm, int ldc,
                            int nc2, const int* cx_in, int* cx_out) {
   const hq_device_info* dev = &w->ds->dev;
@@ -706,9 +816,14 @@ static int core_hqrrp_k(hq_ws* w, int m, int n, double* dA, int ldda, int* djpvt
     /* Panel QR (pivoted within its b columns), U, tau. */
     /* Mixed: squared column norms in the panel's pivoting (division-free
      * LAWN 176 downdate); plain keeps LAPACK's formula. */
-    CK(hq_panel_qrp(w->st, dev, mp, b, panel_piv, ABR, ldda, dtau + j, w->U, w->ldu, w->perm,
-                    w->part, w->part_elems, w->rowbuf, w->bar + 1, w->err, spin, w->mixed,
-                    w->ut));
+    const int use_gram = w->gram && w->gQ && !w->ut && b <= HQ_GRAM_MAX;
+    if (use_gram) {
+      int rc = gram_panel(w, m, j, b, panel_piv, AR, ldda, djpvt + j, dtau + j);
+      if (rc) return rc;
+    }
+    CK(hq_panel_qrp_fallback(w->st, dev, mp, b, panel_piv, ABR, ldda, dtau + j, w->U, w->ldu,
+                             w->perm, w->part, w->part_elems, w->rowbuf, w->bar + 1, w->err,
+                             spin, w->mixed, w->ut, use_gram ? w->gstat : NULL));
     if (w->mixed) CK(hq_set_diag(w->st, b, w->U, w->ldu, 0.0)); /* U' for the digit products */
     /* The panel's swaps on the rows above it and on the labels. */
     CK(hq_permute_cols(w->st, j, AR, ldda, b, w->perm, w->tmp, djpvt + j, w->label_tmp));

@@ -1213,7 +1213,12 @@ extern "C" int hq_ozk_split(cudaStream_t stream, const double* X, long long rs, 
   if (blocks > 4096) blocks = 4096;
   uint8_t* t = static_cast<uint8_t*>(tiles);
   constexpr int ROW_CPT = 4;
-  if (K > 512 * 8 * ROW_CPT && S == 7) {
+  // Long rows (K > 16384), or fewer than FEW_ROWS rows of 512 or more (the
+  // one-pass kernel's 8-row CTAs would then number fewer than a GB300's 152
+  // SMs, each warp walking a long row), take the two-pass split, which
+  // spreads every row over CTAs.
+  constexpr int FEW_ROWS = 8 * 152;
+  if (S == 7 && (K > 512 * 8 * ROW_CPT || (K >= 512 && rows_total < FEW_ROWS))) {
     int mblocks = rows_total < 8192 ? rows_total : 8192;
     ozk_rowmax_kernel<<<mblocks, 256, 0, stream>>>(X, rs, ks, R, K, rows_total, exps);
     const long long chunks = (long long)rows_total * KB * (TK / 8);

@@ -50,7 +50,8 @@ __global__ void gather_perm(int rows, const double* __restrict__ X, int ldx,
                             const int* __restrict__ labels, int* __restrict__ label_tmp) {
   const int k = blockIdx.y;
   const int src = perm[k];
-  if (src < 0 || src >= (int)gridDim.y) return;
+  // A column that stays in place is neither gathered nor scattered.
+  if (src < 0 || src >= (int)gridDim.y || src == k) return;
   const double* s = X + (size_t)src * ldx;
   double* t = tmp + (size_t)k * rows;
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x)
@@ -62,7 +63,7 @@ __global__ void scatter_perm(int rows, double* __restrict__ X, int ldx,
                              const int* __restrict__ perm, const double* __restrict__ tmp,
                              int* __restrict__ labels, const int* __restrict__ label_tmp) {
   const int k = blockIdx.y;
-  if (perm[k] < 0 || perm[k] >= (int)gridDim.y) return;
+  if (perm[k] < 0 || perm[k] >= (int)gridDim.y || perm[k] == k) return;
   double* d = X + (size_t)k * ldx;
   const double* t = tmp + (size_t)k * rows;
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x)

@@ -63,6 +63,7 @@ struct PnArgs {
   int smem_mode, rloc_max, ldxs;
   int sqnorm;  // keep squared norms (d^2 <- d^2 - r^2, LAWN 176's test without divisions)
   int ut;      // UT-transform convention: a zero tail gives H = I - 2 e e^T (tau 2, beta -alpha)
+  const int* gram_stat;  // non-null: skip when *gram_stat == 0 (the Gram panel succeeded)
 };
 
 // Fixed-point stage sums (hq_fixedpoint.h): words 0..2 of a column are the
@@ -105,6 +106,8 @@ __device__ __forceinline__ void pick(long long key, int k, long long& bkey, int&
 
 __global__ void __launch_bounds__(NT, 1) panel_qrp_kernel(PnArgs a) {
   extern __shared__ __align__(16) double smem[];
+  // Every CTA reads the same word, written before the launch.
+  if (a.gram_stat != nullptr && *a.gram_stat == 0) return;
   const int G = gridDim.x, cta = blockIdx.x, tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
   const int nc = a.nc;
@@ -569,6 +572,16 @@ extern "C" int hq_panel_qrp(cudaStream_t stream, const hq_device_info* dev, int 
                             double* U, int ldu, int* perm, double* part, size_t part_elems,
                             double* rowbuf, unsigned* bar, int* err, unsigned spin_limit,
                             int sqnorm, int ut) {
+  return hq_panel_qrp_fallback(stream, dev, mp, nc, pivoting, P, ldp, tau, U, ldu, perm, part,
+                               part_elems, rowbuf, bar, err, spin_limit, sqnorm, ut, nullptr);
+}
+
+extern "C" int hq_panel_qrp_fallback(cudaStream_t stream, const hq_device_info* dev, int mp,
+                                     int nc, int pivoting, double* P, int ldp, double* tau,
+                                     double* U, int ldu, int* perm, double* part,
+                                     size_t part_elems, double* rowbuf, unsigned* bar, int* err,
+                                     unsigned spin_limit, int sqnorm, int ut,
+                                     const int* gram_stat) {
   if (nc <= 0 || mp <= 0) return 0;
   if (nc > HQ_MAX_PANEL) return (int)cudaErrorInvalidValue;
   PnArgs a;
@@ -590,6 +603,7 @@ extern "C" int hq_panel_qrp(cudaStream_t stream, const hq_device_info* dev, int 
   a.spin_limit = spin_limit;
   a.sqnorm = sqnorm;
   a.ut = ut;
+  a.gram_stat = gram_stat;
   const int G = panel_grid(dev, mp);
   if (HQ_PANEL_PART_ELEMS(G, nc) > part_elems) return (int)cudaErrorInvalidValue;
   a.acc = reinterpret_cast<unsigned long long*>(part + (size_t)2 * G * a.pstride);

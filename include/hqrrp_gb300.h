@@ -267,6 +267,14 @@ unsigned long long hqrrp_gb300_launch_count(void);
  * fault injection for testing callers' error paths. */
 unsigned long long hqrrp_gb300_pool_alloc_count(void);
 
+/* Mixed precision's panels: of the last call that factored panels in mixed
+ * precision, how many the Gram panel committed (Gram matrix, pivoted
+ * CholeskyQR2, Householder reconstruction) and how many it passed on to the
+ * column-by-column pivoted panel (a Cholesky or LU pivot that showed the
+ * panel too ill-conditioned for it).  Synchronizes the device.  Setting
+ * HQRRP_GB300_GRAM_PANEL=0 in the environment turns the Gram panel off. */
+int hqrrp_gb300_gram_panel_counts(int* committed, int* fallback);
+
 /* Message of the last failure on the calling thread ("" if none). */
 const char* hqrrp_gb300_last_error(void);
 
