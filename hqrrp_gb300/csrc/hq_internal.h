@@ -79,23 +79,39 @@ size_t hq_panel_part_elems(const hq_device_info* dev, int nc);
 #define HQ_GRAM_MAX 128
 /* Pass 1: pivoted Cholesky of G (lower triangle read) scaled to unit
  * diagonal, in FP32: perm[k] = source column of position k, R (FP64, upper)
- * with R^T R ~ P^T G P; *stat := 0, or bit with R = I, perm = identity. */
+ * with R^T R ~ P^T G P; *stat := 0, or bit with R = I, perm = identity;
+ * *alt, *emax := 0. */
 int hq_gram_pchol32(cudaStream_t stream, int n, const double* G, int ldg, double* R, int ldr,
-                    int* perm, int* stat, int bit);
+                    int* perm, int* stat, int bit, int* alt, unsigned long long* emax);
 /* FP64 on a cluster of eight CTAs.  mode 0: Cholesky of the symmetric A
  * (lower triangle read), F := R upper.  mode 1: LU without pivoting of A - D
  * (Householder reconstruction), F := L strictly below the diagonal and U on
  * and above, dsgn := D, tau := -D U_kk.  A bad pivot sets bit in *stat and
- * gives identity factors. */
+ * gives identity factors.  gate (may be NULL): skipped when *gate == 0. */
 int hq_cluster_fact(cudaStream_t stream, int n, int mode, const double* A, int lda, double* F,
-                    int ldf, double* dsgn, double* tau, int* stat, int bit);
-/* mode 0: X = A^{-1}; mode 1: X = diag(rs) A B (rs may be NULL); A, B upper. */
+                    int ldf, double* dsgn, double* tau, int* stat, int bit, const int* gate);
+/* Second CholeskyQR pass for G = I + E near the identity (FP64, no
+ * sequential factorization): R (= I + X, upper) and Rinv = R^{-1} by a fixed
+ * number of fixed-point steps over b x b products; wX, wZ are b x b work
+ * matrices (all with leading dimension ld); *emax receives max|E| (as the
+ * bits of a double), which sets the number of steps.  Sets *alt when max|E|
+ * is too large for the steps to converge (R and Rinv are then left to
+ * kernels gated on *alt). */
+int hq_nearid_chol(cudaStream_t stream, int n, const double* G, int ldg, double* R, double* Rinv,
+                   double* wX, double* wZ, int ld, int* alt, unsigned long long* emax);
+/* mode 0: X = A^{-1}; mode 1: X = diag(rs) A B (rs may be NULL); A, B upper.
+ * gate (may be NULL): skipped when *gate == 0. */
 int hq_tri(cudaStream_t stream, int n, int mode, const double* A, int lda, const double* B,
-           int ldb, const double* rs, double* X, int ldx);
+           int ldb, const double* rs, double* X, int ldx, const int* gate);
 /* Two independent such jobs in one launch (mode1 = -1: the first only). */
 int hq_tri2(cudaStream_t stream, int n, int mode0, const double* A0, int lda0, const double* B0,
             int ldb0, const double* rs0, double* X0, int ldx0, int mode1, const double* A1,
             int lda1, const double* B1, int ldb1, const double* rs1, double* X1, int ldx1);
+/* The same, skipped when gate is not NULL and *gate == 0. */
+int hq_tri2g(cudaStream_t stream, int n, int mode0, const double* A0, int lda0, const double* B0,
+             int ldb0, const double* rs0, double* X0, int ldx0, int mode1, const double* A1,
+             int lda1, const double* B1, int ldb1, const double* rs1, double* X1, int ldx1,
+             const int* gate);
 /* When *stat == 0: the panel P (mp x n) := R (RH's upper triangle) and the
  * Householder vectors (LU's strict lower part; U's rows >= n), U's top rows
  * := explicit unit-lower V1, tau := tau_in, perm := identity.  count (may be

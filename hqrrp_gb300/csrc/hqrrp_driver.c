@@ -220,7 +220,8 @@ typedef struct {
    * the LU of Q11 - D, and R; gstat is the panel's status word. */
   int gram;
   double *gQ, *gG, *gR1, *gR2, *gRi, *gLU, *gRH, *gsgn, *gtau;
-  int *gperm, *gstat, *gcount; /* gcount: panels committed, panels passed on */
+  int *gperm, *gstat, *galt, *gcount; /* gcount: panels committed, panels passed on */
+  unsigned long long* gemax;           /* the second pass's max|G2 - I| (double bits) */
   int ph_override; /* >= 0: charge split-product intervals to this phase */
 } hq_ws;
 
@@ -468,8 +469,8 @@ static int ws_setup(hq_ws* w, int m, int n, int nb, int pp, int pw) {
     if (w->gram) {
       const size_t sq = (size_t)HQ_GRAM_MAX * HQ_GRAM_MAX;
       w->gQ = ws_alloc(w, sizeof(double) * (size_t)w->ldu * imin(kmax, HQ_GRAM_MAX));
-      double* sm = ws_alloc(w, sizeof(double) * (6 * sq + 2 * HQ_GRAM_MAX));
-      w->gperm = ws_alloc(w, sizeof(int) * (HQ_GRAM_MAX + 3));
+      double* sm = ws_alloc(w, sizeof(double) * (6 * sq + 2 * HQ_GRAM_MAX + 1));
+      w->gperm = ws_alloc(w, sizeof(int) * (HQ_GRAM_MAX + 4));
       if (sm && w->gperm) {
         w->gG = sm;
         w->gR1 = sm + sq;
@@ -479,8 +480,10 @@ static int ws_setup(hq_ws* w, int m, int n, int nb, int pp, int pw) {
         w->gRH = sm + 5 * sq;
         w->gsgn = sm + 6 * sq;
         w->gtau = w->gsgn + HQ_GRAM_MAX;
+        w->gemax = (unsigned long long*)(w->gtau + HQ_GRAM_MAX);
         w->gstat = w->gperm + HQ_GRAM_MAX;
-        w->gcount = w->gstat + 1;
+        w->galt = w->gstat + 1;
+        w->gcount = w->gstat + 2;
       }
     }
   }
@@ -654,24 +657,30 @@ static int gram_panel(hq_ws* w, int m, int j, int b, int piv, double* AR, int ld
   rc = ozk_product(w, S, b, b, mp, ABR, ldda, 1, ABR, ldda, 1, 0, 1.0, w->gG, 1, L);
   if (rc) return rc;
   if (piv) {
-    CK(hq_gram_pchol32(w->st, b, w->gG, L, w->gR1, L, w->gperm, w->gstat, 1));
+    CK(hq_gram_pchol32(w->st, b, w->gG, L, w->gR1, L, w->gperm, w->gstat, 1, w->galt,
+                       w->gemax));
   } else {
     CK(hq_fill_iota(w->st, w->gperm, b, 0));
-    CK(cudaMemsetAsync(w->gstat, 0, sizeof(int), w->st));
-    CK(hq_cluster_fact(w->st, b, 0, w->gG, L, w->gR1, L, NULL, NULL, w->gstat, 1));
+    CK(cudaMemsetAsync(w->gstat, 0, 2 * sizeof(int), w->st)); /* gstat, galt */
+    CK(cudaMemsetAsync(w->gemax, 0, sizeof(unsigned long long), w->st));
+    CK(hq_cluster_fact(w->st, b, 0, w->gG, L, w->gR1, L, NULL, NULL, w->gstat, 1, NULL));
   }
-  CK(hq_tri(w->st, b, 0, w->gR1, L, NULL, 0, NULL, w->gRi, L));
+  CK(hq_tri(w->st, b, 0, w->gR1, L, NULL, 0, NULL, w->gRi, L, NULL));
   CK(hq_permute_cols(w->st, m, AR, ldda, b, w->gperm, w->tmp, jp, w->label_tmp));
   /* Q1 = Ap P R1^{-1}; G2 = Q1^T Q1; R2; Q = Q1 R2^{-1} (in place) */
   rc = ozk_product(w, S, mp, b, b, ABR, 1, ldda, w->gRi, L, 1, 0, 1.0, w->gQ, 1, w->ldu);
   if (!rc) rc = ozk_product(w, S, b, b, mp, w->gQ, w->ldu, 1, w->gQ, w->ldu, 1, 0, 1.0, w->gG, 1, L);
   if (rc) return rc;
-  CK(hq_cluster_fact(w->st, b, 0, w->gG, L, w->gR2, L, NULL, NULL, w->gstat, 2));
-  CK(hq_tri(w->st, b, 0, w->gR2, L, NULL, 0, NULL, w->gRi, L));
+  /* R2 and R2^{-1}: fixed-point steps when G2 is near the identity, else
+   * (galt set by the first step) the cluster Cholesky and an inverse */
+  CK(hq_nearid_chol(w->st, b, w->gG, L, w->gR2, w->gRi, w->gLU, w->gRH, L, w->galt,
+                    w->gemax));
+  CK(hq_cluster_fact(w->st, b, 0, w->gG, L, w->gR2, L, NULL, NULL, w->gstat, 2, w->galt));
+  CK(hq_tri(w->st, b, 0, w->gR2, L, NULL, 0, NULL, w->gRi, L, w->galt));
   rc = ozk_product(w, S, mp, b, b, w->gQ, 1, w->ldu, w->gRi, L, 1, 0, 1.0, w->gQ, 1, w->ldu);
   if (rc) return rc;
   /* Q11 - D = L U; R = D R2 R1; V2 = Q2 U^{-1} (into U's rows >= b) */
-  CK(hq_cluster_fact(w->st, b, 1, w->gQ, w->ldu, w->gLU, L, w->gsgn, w->gtau, w->gstat, 4));
+  CK(hq_cluster_fact(w->st, b, 1, w->gQ, w->ldu, w->gLU, L, w->gsgn, w->gtau, w->gstat, 4, NULL));
   /* R_H = D R2 R1 and U^{-1}, one launch */
   CK(hq_tri2(w->st, b, 1, w->gR2, L, w->gR1, L, w->gsgn, w->gRH, L, mp > b ? 0 : -1, w->gLU, L,
              NULL, 0, NULL, w->gRi, L));

@@ -58,58 +58,51 @@ constexpr int CT = 512;          // threads of the one-SM kernels
 constexpr int CW = CT / 32;
 constexpr int TW = 4;            // warps per CTA of the triangular kernel (one column per CTA)
 constexpr float PIVOT32_REL_MIN = 1e-5f;  // first pass: scaled pivot floor
-constexpr double CHOL2_REL_MIN = 1e-10;   // second pass: pivot floor, relative to the diagonal
+constexpr double CHOL2_REL_MIN = 1e-10;   // cluster Cholesky: pivot floor, relative to the diagonal
+constexpr double NEARID_MAX = 2e-4;       // second pass: largest max|G2 - I| it converges from
+constexpr int NEARID_ITERS = 4;           // second pass: fixed-point steps
 constexpr int CL = 8;                     // CTAs of the cluster kernels
 constexpr int CLT = 256;                  // threads per CTA of the cluster kernels
 constexpr int CLW = CLT / 32;
 constexpr int OWN = GN / CL;              // columns per CTA (column j lives in CTA j % CL)
 static_assert(OWN == 2 * CLW, "each warp of a cluster CTA updates two own columns");
 
-// Scalars of pivoted-Cholesky step k from its scaled pivot d (one thread):
-// bad[k], 1/d, R_kk = sqrt(d), 1/R_kk.
-__device__ __forceinline__ void pchol_scalars(float d, int k, int* bad, float* dinv, float* r,
-                                              float* rinv) {
-  const int b = !(d > PIVOT32_REL_MIN);  // also NaN and a zero column
-  bad[k] = b;
-  const float dd = b ? 1.0f : d;
-  dinv[k] = 1.0f / dd;
-  r[k] = sqrtf(dd);
-  rinv[k] = 1.0f / r[k];
-}
-
-// Pass 1: pivoted Cholesky of the n x n Gram matrix G (lower triangle read,
-// ldg) scaled to unit diagonal, in FP32 on one SM.  The pivot is the largest
-// residual norm: scaled Schur diagonal times the column's original squared
-// norm (relative to the largest, in FP32), first on ties.  Writes perm[k]
-// (source column of position k) and R = Rs diag(sqrt(G_pp)) in FP64 (upper,
-// zeros below), Rs the scaled factor; *stat = 0, or `bit` with R = I and
-// perm = identity when a scaled pivot is not above PIVOT32_REL_MIN.
-//
-// Step k: every warp finds the argmax; barrier; the thread that swaps the
-// diagonal (k and p, as LAPACK's dpstrf does on lower storage) computes the
-// step's scalars while column k-1 is scaled; barrier; the trailing triangle
-// is updated from the unscaled column k; barrier.
+// Pass 1: pivoted Cholesky of the n x n Gram matrix G (ldg) scaled to unit
+// diagonal, in FP32 on one SM, the matrix held in registers.  Thread (warp
+// w, lane t) holds the 32 entries (i, j) with i = t + 32 a (a < 4) and
+// j = w + 16 c (c < 8) of the full symmetric matrix.  Columns are not moved:
+// step k picks the active column p with the largest residual norm (scaled
+// Schur diagonal times the column's original squared norm relative to the
+// largest; the lowest index among residuals equal to 2^-15), the warp holding column p publishes
+// l = S[:, p] / sqrt(S[p][p]) over the active rows (0 elsewhere), and every
+// thread updates its entries by S_ij -= l_i l_j -- a no-op on eliminated
+// rows and columns, so the update needs no masks.  Three barriers per step.
+// Writes perm[k] (source column of position k) and R = Rs diag(sqrt(G_pp))
+// in FP64 (upper, zeros below), Rs the scaled factor; *stat = 0, or `bit`
+// with R = I and perm = identity when a scaled pivot is not above
+// PIVOT32_REL_MIN; *alt (the second pass's choice of method) and *emax
+// (its max|E|) := 0.
 __global__ void __launch_bounds__(CT, 1)
     gram_pchol32_kernel(int n, const double* __restrict__ G, int ldg, double* __restrict__ R,
-                        int ldr, int* __restrict__ perm, int* __restrict__ stat, int bit) {
-  extern __shared__ float Sf[];  // LDS * n
+                        int ldr, int* __restrict__ perm, int* __restrict__ stat, int bit,
+                        int* __restrict__ alt, unsigned long long* __restrict__ emax) {
+  extern __shared__ float s_Rp[];  // GN * GN: s_Rp[k * GN + i] = row k of Rs at source column i
   __shared__ double s_sc[GN], s_rt[GN];
-  __shared__ float s_key[GN], s_dinv[GN], s_r[GN], s_rinv[GN], s_wmax[CW];
-  __shared__ int s_perm[GN], s_bad[GN];
+  __shared__ float s_key[GN], s_d[GN], s_l[GN], s_r[GN], s_wmax[CW];
+  __shared__ int s_ord[GN], s_act[GN], s_bad;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  float dmax = 0.0f;
-  for (int j = tid; j < n; j += CT) {
-    const double d = G[j + (size_t)j * ldg];
-    const int ok = d > 0.0 && d <= 1.7e308;
+  static_assert(CT == 512 && GN == 128, "register layout: 16 warps x 32 lanes, 4 x 8 entries");
+  for (int j = tid; j < GN; j += CT) {
+    double d = 0.0;
+    if (j < n) d = G[j + (size_t)j * ldg];
+    const int ok = j < n && d > 0.0 && d <= 1.7e308;
     const double rt = ok ? sqrt(d) : 0.0;
     s_rt[j] = rt;
     s_sc[j] = ok ? 1.0 / rt : 0.0;
-    s_perm[j] = j;
-    // the squared norm relative to 2^-1000: FP32 keys need a common scale
-    s_key[j] = ok ? (float)log2(d) : -2048.0f;
+    s_key[j] = ok ? (float)log2(d) : -4096.0f;  // squared norm, scaled below
+    s_act[j] = j < n;
   }
   __syncthreads();
-  // keys: 2^(log2 d - max log2 d), i.e. d / max d, computed without overflow
   if (warp == 0) {
     float m = -4096.0f;
     for (int j = lane; j < n; j += 32) m = fmaxf(m, s_key[j]);
@@ -118,136 +111,115 @@ __global__ void __launch_bounds__(CT, 1)
     if (lane == 0) s_wmax[0] = m;
   }
   __syncthreads();
-  dmax = s_wmax[0];
-  __syncthreads();
-  for (int j = tid; j < n; j += CT) s_key[j] = exp2f(s_key[j] - dmax);
-  for (int j = warp; j < n; j += CW) {
+  const float kmax = s_wmax[0];
+  for (int j = tid; j < n; j += CT) s_key[j] = exp2f(s_key[j] - kmax);  // d_j / max d
+  float S[4][8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    const int j = warp + 16 * c;
     double v[4];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int i = lane + 32 * q;
-      v[q] = (i >= j && i < n) ? G[i + (size_t)j * ldg] : 0.0;
+    for (int a = 0; a < 4; ++a) {
+      const int i = lane + 32 * a;
+      v[a] = (i < n && j < n) ? G[i + (size_t)j * ldg] : 0.0;
     }
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int i = lane + 32 * q;
-      if (i >= j && i < n) Sf[i + j * LDS] = (float)(v[q] * s_sc[i] * s_sc[j]);
+    for (int a = 0; a < 4; ++a) {
+      const int i = lane + 32 * a;
+      S[a][c] = (i < n && j < n) ? (float)(v[a] * s_sc[i] * s_sc[j]) : 0.0f;
+      if (i == j) s_d[j] = S[a][c];
     }
   }
   __syncthreads();
 
   int fail = 0;
   for (int k = 0; k < n; ++k) {
-    // argmax of key_j * Sf[j][j] over j >= k, first on ties (every warp)
-    float best = -1.0f;
-    int p = n;
-    for (int j = k + lane; j < n; j += 32) {
-      const float v = s_key[j] * Sf[j + j * LDS];
-      if (v > best) {
-        best = v;
-        p = j;
-      }
-    }
+    // Warp 0: the pivot and its scalars.  One 32-bit key per column: the
+    // residual's FP32 bits above the low 8 (positive floats order like their
+    // bits) and 255 - j below them, so one warp maximum gives the largest
+    // residual and, among residuals equal to 2^-15, the lowest column; 0 =
+    // no active column.
+    if (warp == 0) {
+      unsigned best = 0u;
 #pragma unroll
-    for (int o = 16; o; o >>= 1) {
-      const float ob = __shfl_xor_sync(0xffffffffu, best, o);
-      const int oi = __shfl_xor_sync(0xffffffffu, p, o);
-      if (ob > best || (ob == best && oi < p)) {
-        best = ob;
-        p = oi;
-      }
-    }
-    if (p >= n) {
-      fail = 1;
-      break;
-    }
-    __syncthreads();  // the swap below rewrites the diagonal the argmax read
-    const int sw = p != k;
-    if (k > 0) {
-      const float rinv = s_rinv[k - 1];
-      for (int i = k + tid; i < n; i += CT)
-        if (!sw || (i != k && i != p)) Sf[i + (k - 1) * LDS] *= rinv;
-      if (sw && tid == k - 1) {
-        Sf[k + (k - 1) * LDS] *= rinv;
-        Sf[p + (k - 1) * LDS] *= rinv;
-      }
-    }
-    if (tid == k) pchol_scalars(Sf[p + p * LDS], k, s_bad, s_dinv, s_r, s_rinv);
-    if (sw) {
-      for (int t = tid; t < n; t += CT) {
-        float* a = nullptr;
-        float* b = nullptr;
-        if (t < k) {
-          a = &Sf[k + t * LDS];
-          b = &Sf[p + t * LDS];
-        } else if (t == k) {
-          a = &Sf[k + k * LDS];
-          b = &Sf[p + p * LDS];
-          const int pi = s_perm[k];
-          s_perm[k] = s_perm[p];
-          s_perm[p] = pi;
-          const float ky = s_key[k];
-          s_key[k] = s_key[p];
-          s_key[p] = ky;
-          const double rt = s_rt[k];
-          s_rt[k] = s_rt[p];
-          s_rt[p] = rt;
-        } else if (t < p) {
-          a = &Sf[t + k * LDS];
-          b = &Sf[p + t * LDS];
-        } else if (t > p) {
-          a = &Sf[t + k * LDS];
-          b = &Sf[t + p * LDS];
+      for (int q = 0; q < 4; ++q) {
+        const int j = lane + 32 * q;
+        if (j < n && s_act[j]) {
+          const float v = s_key[j] * s_d[j];
+          const unsigned vb = v > 0.0f ? __float_as_uint(v) : 0u;  // NaN and v <= 0: lowest
+          best = max(best, (vb & ~255u) | (unsigned)(255 - j));
         }
-        if (a) {
-          const float x = *a;
-          *a = *b;
-          *b = x;
-        }
+      }
+      best = __reduce_max_sync(0xffffffffu, best);
+      const int bp = best ? 255 - (int)(best & 255u) : n;
+      if (lane == 0) {
+        const float d = bp < n ? s_d[bp] : 0.0f;
+        const int bad = !(d > PIVOT32_REL_MIN);  // also NaN and a zero column
+        s_bad = bad;
+        s_r[k] = bad ? 1.0f : sqrtf(d);
+        s_ord[k] = bp < n ? bp : 0;
+        if (bp < n) s_act[bp] = 0;
       }
     }
     __syncthreads();
-    if (s_bad[k]) {
+    if (s_bad) {
       fail = 1;
       break;
     }
-    // Trailing update, two columns per warp at a time with their four row
-    // chunks unrolled (sixteen independent shared-memory loads in flight).
-    const float dinv = s_dinv[k];
-    for (int j = k + 1 + warp; j < n; j += 2 * CW) {
-      const int j2 = j + CW;
-      const float l1 = Sf[j + k * LDS] * dinv;
-      const float l2 = j2 < n ? Sf[j2 + k * LDS] * dinv : 0.0f;
-      float a1[4], b1[4], a2[4], b2[4];
+    const int p = s_ord[k];
+    // The warp holding column p publishes l over the active rows.
+    if (warp == (p & 15)) {
+      const int cp = p >> 4;
+      const float rinv = 1.0f / s_r[k];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int i1 = j + lane + 32 * q, i2 = j2 + lane + 32 * q;
-        a1[q] = i1 < n ? Sf[i1 + k * LDS] : 0.0f;
-        b1[q] = i1 < n ? Sf[i1 + j * LDS] : 0.0f;
-        a2[q] = i2 < n ? Sf[i2 + k * LDS] : 0.0f;
-        b2[q] = i2 < n ? Sf[i2 + j2 * LDS] : 0.0f;
-      }
+      for (int a = 0; a < 4; ++a) {
+        float v = S[a][0];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int i1 = j + lane + 32 * q, i2 = j2 + lane + 32 * q;
-        if (i1 < n) Sf[i1 + j * LDS] = b1[q] - a1[q] * l1;
-        if (i2 < n) Sf[i2 + j2 * LDS] = b2[q] - a2[q] * l2;
+        for (int c = 1; c < 8; ++c)
+          if (c == cp) v = S[a][c];
+        const int i = lane + 32 * a;
+        const float l = (i < n && s_act[i]) ? v * rinv : 0.0f;
+        s_l[i] = l;
+        s_Rp[k * GN + i] = l;
       }
+    }
+    __syncthreads();
+    float li[4], lj[8];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) li[a] = s_l[lane + 32 * a];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) lj[c] = s_l[warp + 16 * c];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int c = 0; c < 8; ++c) S[a][c] = fmaf(-li[a], lj[c], S[a][c]);
+    // Diagonal entries: lane w + 16 h of warp w holds (i, i) for
+    // i = lane + 32 a in slot c = 2 a + h.
+    if ((lane & 15) == warp) {
+      const int h = lane >> 4;
+#pragma unroll
+      for (int a = 0; a < 4; ++a) s_d[lane + 32 * a] = h ? S[a][2 * a + 1] : S[a][2 * a];
     }
     __syncthreads();
   }
-  // Column n-2 was scaled in the last step; column n-1 has no rows below.
-  for (int j = warp; j < n; j += CW)
-    for (int i = lane; i < n; i += 32) {
+  // R[k][m] = Rs[k][m] sqrt(G_pp), p = perm[m]: row k of Rs at source column p.
+  for (int m = warp; m < n; m += CW)
+    for (int k = lane; k < n; k += 32) {
       double v;
       if (fail)
-        v = i == j ? 1.0 : 0.0;
+        v = k == m ? 1.0 : 0.0;
+      else if (k < m)
+        v = (double)s_Rp[k * GN + s_ord[m]] * s_rt[s_ord[m]];
       else
-        v = i < j ? (double)Sf[j + i * LDS] * s_rt[j] : (i == j ? (double)s_r[j] * s_rt[j] : 0.0);
-      R[i + (size_t)j * ldr] = v;
+        v = k == m ? (double)s_r[m] * s_rt[s_ord[m]] : 0.0;
+      R[k + (size_t)m * ldr] = v;
     }
-  for (int k = tid; k < n; k += CT) perm[k] = fail ? k : s_perm[k];
-  if (tid == 0) *stat = fail ? bit : 0;
+  for (int k = tid; k < n; k += CT) perm[k] = fail ? k : s_ord[k];
+  if (tid == 0) {
+    *stat = fail ? bit : 0;
+    *alt = 0;
+    *emax = 0ull;
+  }
 }
 
 // Pivot scalars of a cluster factorization step, from the updated diagonal
@@ -268,7 +240,15 @@ __device__ __forceinline__ void cluster_scalars(int mode, double q, double d0, d
     piv = bad ? 1.0 : u;
   }
   out[0] = piv;
-  out[1] = 1.0 / piv;
+  // 1 / piv: an FP32 quotient refined by two Newton steps y += y (1 - piv y)
+  // (2^-24 -> 2^-48 -> FP64 rounding), four dependent FMAs instead of the
+  // longer FP64 division sequence on this critical path; piv lies in
+  // [0.5, 2.5] (LU) or is a square root of a diagonal entry well inside
+  // FP32's range (Cholesky of a scaled Gram matrix).
+  double y = (double)(1.0f / (float)piv);
+  y = fma(y, fma(-piv, y, 1.0), y);
+  y = fma(y, fma(-piv, y, 1.0), y);
+  out[1] = y;
   out[2] = D;
   out[3] = bad ? 1.0 : 0.0;
 }
@@ -285,13 +265,16 @@ __device__ __forceinline__ void cluster_scalars(int mode, double q, double d0, d
 // owner of column k + 1 updates that column first, takes its pivot scalars,
 // scales it and writes it into every CTA's receive buffer (distributed
 // shared memory, double-buffered by the parity of the step).  One cluster
-// barrier per step, which also orders the receive buffers' reuse.  A bad
+// barrier per step, split into arrive and wait around the update of the
+// remaining own columns; it also orders the receive buffers' reuse.  A bad
 // pivot is recorded and replaced by 1, so every CTA takes the same barriers;
 // the output is then the identity (and tau 0) and `bit` is set in *stat.
 __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CLT, 1)
     cluster_fact_kernel(int n, int mode, const double* __restrict__ A, int lda,
                         double* __restrict__ F, int ldf, double* __restrict__ dsgn,
-                        double* __restrict__ tau, int* __restrict__ stat, int bit) {
+                        double* __restrict__ tau, int* __restrict__ stat, int bit,
+                        const int* __restrict__ gate) {
+  if (gate != nullptr && *gate == 0) return;  // every CTA of the cluster reads the same word
   cg::cluster_group cl = cg::this_cluster();
   const int rank = (int)cl.block_rank();
   __shared__ double Xc[OWN * LDS];
@@ -350,7 +333,6 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CLT, 1)
   int bad = 0;
   for (int k = 0; k < n; ++k) {
     const int b = k & 1;
-    bad |= scal[b][3] != 0.0;
     const int nx = k + 1;
     if (nx < n && nx % CL == rank) {
       const int c1 = nx / CL;
@@ -364,7 +346,10 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CLT, 1)
       publish(nx, b ^ 1);
     }
     // The other own columns right of k: warp w takes local columns w and
-    // w + CLW together, their four row chunks unrolled.
+    // w + CLW together, their four row chunks unrolled.  Everything read
+    // from the receive buffer is in registers before this CTA arrives at the
+    // step's barrier (after which the buffer may be refilled two steps on),
+    // so the barrier's latency overlaps the update; the wait comes last.
     {
       double xa[2][4], lb[2][4], mult[2];
       int act[2], base[2];
@@ -384,6 +369,8 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CLT, 1)
           xa[u][q] = live ? Xc[i + c * LDS] : 0.0;
           lb[u][q] = live ? colbuf[b][i] : 0.0;
         }
+      bad |= scal[b][3] != 0.0;
+      cl.barrier_arrive();
 #pragma unroll
       for (int u = 0; u < 2; ++u)
 #pragma unroll
@@ -392,7 +379,8 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CLT, 1)
           if (act[u] && i < n) Xc[i + c * LDS] = xa[u][q] - lb[u][q] * mult[u];
         }
     }
-    cl.sync();
+    __syncthreads();  // the CTA's own updates (after its arrive) before the next step reads them
+    cl.barrier_wait();
   }
   // Output of the own columns.
   for (int c = warp; c < nown; c += CLW) {
@@ -417,6 +405,134 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CLT, 1)
   if (bad && rank == 0 && tid == 0) atomicOr(stat, bit);
 }
 
+// E_ij (i <= j) of G = I + E, read from G's upper triangle (column j is
+// contiguous: coalesced loads).
+__device__ __forceinline__ double e_upper(const double* __restrict__ G, int ldg, int i, int j) {
+  const double g = G[i + (size_t)j * ldg];
+  return i < j ? g : g - 1.0;
+}
+
+// Fixed-point steps the second pass needs from max|E|: the error of R^{-1}
+// after m steps is about max|E|^(m+1) (measured on FP32-preconditioned
+// panels), below 2^-53 after 2 steps up to 4e-6, 3 up to 5e-5, 4 up to
+// NEARID_MAX.
+__device__ __forceinline__ int nearid_steps(double emax) {
+  return emax <= 4e-6 ? 2 : (emax <= 5e-5 ? 3 : NEARID_ITERS);
+}
+
+// One step of the second CholeskyQR pass for G = I + E near the identity:
+// R2 = I + X (X upper with its diagonal) and R2^{-1} = I + Z are the fixed
+// points of
+//   X <- Uh(E - X^T X),   Z <- -X (I + Z),
+// Uh = strict upper part plus half the diagonal (X + X^T + X^T X = E is
+// R2^T R2 = G).  Both converge linearly at a rate of about ||E||_2, so
+// NEARID_ITERS steps from X = Uh(E), Z = -X reach working precision when
+// max|E| <= NEARID_MAX (first pass in FP32: max|E| ~ 1e-6 .. 1e-4 for
+// panels with condition numbers 10 .. 300); fewer suffice for smaller
+// max|E| (nearid_steps), and the later launches then only copy.  Every product is a column of a
+// b x b product, so the pass needs no sequential factorization: one CTA per
+// column c stages X's columns 0..c and each thread accumulates one row.
+// Step 0: X, Z are Uh(E), -Uh(E) (Xin, Zin unused), and the CTA checks its
+// column of E against NEARID_MAX, setting *alt when it is exceeded (the
+// later steps then return at once and the cluster Cholesky and a triangular
+// inverse, gated on *alt, take the pass) and raising *emax; the last step
+// writes I + X and I + Z.
+__global__ void __launch_bounds__(TW * 32)
+    nearid_kernel(int n, const double* __restrict__ G, int ldg, const double* __restrict__ Xin,
+                  const double* __restrict__ Zin, int ld, double* __restrict__ Xout,
+                  double* __restrict__ Zout, int it, int* __restrict__ alt,
+                  unsigned long long* __restrict__ emax) {
+  extern __shared__ double sX[];  // LDS * n: X's columns 0..c, rows <= column
+  __shared__ double s_z[GN];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int c = blockIdx.x;
+  const int first = it == 0, last = it == NEARID_ITERS - 1;
+  if (!first) {
+    if (*alt != 0) return;  // too far from the identity: the cluster Cholesky runs
+    if (it >= nearid_steps(__longlong_as_double((long long)*emax))) {
+      // converged: pass X and Z through (adding I after the last step)
+      for (int i = tid; i < n; i += TW * 32) {
+        const double d = (last && i == c) ? 1.0 : 0.0;
+        Xout[i + (size_t)c * ld] = Xin[i + (size_t)c * ld] + d;
+        Zout[i + (size_t)c * ld] = Zin[i + (size_t)c * ld] + d;
+      }
+      return;
+    }
+  }
+  for (int j0 = 4 * warp; j0 <= c; j0 += 4 * TW) {
+    double v[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int j = j0 + a, i = lane + 32 * q;
+        double x = 0.0;
+        if (j <= c && i <= j) {
+          if (first) {
+            const double e = e_upper(G, ldg, i, j);
+            x = i < j ? e : 0.5 * e;
+          } else {
+            x = Xin[i + (size_t)j * ld];
+          }
+        }
+        v[a][q] = x;
+      }
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int j = j0 + a, i = lane + 32 * q;
+        if (j <= c && i <= j) sX[i + j * LDS] = v[a][q];
+      }
+  }
+  for (int k = tid; k <= c; k += TW * 32) {
+    if (first) {
+      const double e = e_upper(G, ldg, k, c);
+      s_z[k] = -(k < c ? e : 0.5 * e);
+      const double ae = fabs(e);
+      if (!(ae <= NEARID_MAX)) atomicOr(alt, 1);  // also NaN
+      // non-negative doubles order like their bits
+      else atomicMax(emax, (unsigned long long)__double_as_longlong(ae));
+    } else {
+      s_z[k] = Zin[k + (size_t)c * ld];
+    }
+  }
+  __syncthreads();
+  for (int i = tid; i < n; i += TW * 32) {
+    double xn = 0.0, zn = 0.0;
+    if (i <= c) {
+      double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+      int k = 0;
+      for (; k + 3 <= i; k += 4) {
+        a0 = fma(sX[k + i * LDS], sX[k + c * LDS], a0);
+        a1 = fma(sX[k + 1 + i * LDS], sX[k + 1 + c * LDS], a1);
+        a2 = fma(sX[k + 2 + i * LDS], sX[k + 2 + c * LDS], a2);
+        a3 = fma(sX[k + 3 + i * LDS], sX[k + 3 + c * LDS], a3);
+      }
+      for (; k <= i; ++k) a0 = fma(sX[k + i * LDS], sX[k + c * LDS], a0);
+      const double e = e_upper(G, ldg, i, c);
+      const double r = e - ((a0 + a1) + (a2 + a3));
+      xn = i < c ? r : 0.5 * r;
+      double b0 = 0.0, b1 = 0.0, b2 = 0.0, b3 = 0.0;
+      k = i;
+      for (; k + 3 <= c; k += 4) {
+        b0 = fma(sX[i + k * LDS], s_z[k], b0);
+        b1 = fma(sX[i + (k + 1) * LDS], s_z[k + 1], b1);
+        b2 = fma(sX[i + (k + 2) * LDS], s_z[k + 2], b2);
+        b3 = fma(sX[i + (k + 3) * LDS], s_z[k + 3], b3);
+      }
+      for (; k <= c; ++k) b0 = fma(sX[i + k * LDS], s_z[k], b0);
+      zn = -sX[i + c * LDS] - ((b0 + b1) + (b2 + b3));
+      if (last && i == c) {
+        xn += 1.0;
+        zn += 1.0;
+      }
+    }
+    Xout[i + (size_t)c * ld] = xn;
+    Zout[i + (size_t)c * ld] = zn;
+  }
+}
+
 // One triangular job: X = A^{-1} (mode 0) or X = diag(rs) A B (mode 1; rs
 // may be null), A and B upper triangular n x n (only their upper triangles
 // are read), X upper triangular with zeros below.
@@ -437,9 +553,11 @@ struct TriJob {
 // lane + 32 q) -- the inverse as a back substitution of axpys, the product
 // as rank-1 column updates.  One column per SM keeps each SM's narrow FP64
 // pipe on one dependent chain.
-__global__ void __launch_bounds__(TW * 32) tri_kernel(int n, TriJob j0, TriJob j1) {
+__global__ void __launch_bounds__(TW * 32)
+    tri_kernel(int n, TriJob j0, TriJob j1, const int* __restrict__ gate) {
   extern __shared__ double sA[];  // LDS * n
   __shared__ double s_dinv[GN];
+  if (gate != nullptr && *gate == 0) return;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const TriJob J = blockIdx.x < (unsigned)n ? j0 : j1;
   const int c = (int)(blockIdx.x % (unsigned)n);
@@ -573,35 +691,69 @@ __global__ void gram_commit_kernel(int mp, int n, double* __restrict__ P, int ld
 }  // namespace
 
 extern "C" int hq_gram_pchol32(cudaStream_t stream, int n, const double* G, int ldg, double* R,
-                               int ldr, int* perm, int* stat, int bit) {
+                               int ldr, int* perm, int* stat, int bit, int* alt,
+                               unsigned long long* emax) {
   if (n <= 0 || n > GN) return (int)cudaErrorInvalidValue;
-  const size_t smem = sizeof(float) * (size_t)LDS * (size_t)n;
+  const size_t smem = sizeof(float) * (size_t)GN * GN;
   cudaError_t e = cudaFuncSetAttribute(gram_pchol32_kernel,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return (int)e;
-  gram_pchol32_kernel<<<1, CT, smem, stream>>>(n, G, ldg, R, ldr, perm, stat, bit);
+  gram_pchol32_kernel<<<1, CT, smem, stream>>>(n, G, ldg, R, ldr, perm, stat, bit, alt,
+                                                emax);
   hq_count_launches(1);
   return (int)cudaGetLastError();
 }
 
 extern "C" int hq_cluster_fact(cudaStream_t stream, int n, int mode, const double* A, int lda,
-                               double* F, int ldf, double* dsgn, double* tau, int* stat, int bit) {
+                               double* F, int ldf, double* dsgn, double* tau, int* stat, int bit,
+                               const int* gate) {
   if (n <= 0 || n > GN || mode < 0 || mode > 1) return (int)cudaErrorInvalidValue;
-  cluster_fact_kernel<<<CL, CLT, 0, stream>>>(n, mode, A, lda, F, ldf, dsgn, tau, stat, bit);
+  cluster_fact_kernel<<<CL, CLT, 0, stream>>>(n, mode, A, lda, F, ldf, dsgn, tau, stat, bit,
+                                              gate);
   hq_count_launches(1);
   return (int)cudaGetLastError();
 }
 
+extern "C" int hq_nearid_chol(cudaStream_t stream, int n, const double* G, int ldg, double* R,
+                              double* Rinv, double* wX, double* wZ, int ld, int* alt,
+                              unsigned long long* emax) {
+  if (n <= 0 || n > GN) return (int)cudaErrorInvalidValue;
+  const size_t smem = sizeof(double) * (size_t)LDS * (size_t)n;
+  cudaError_t e =
+      cudaFuncSetAttribute(nearid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return (int)e;
+  static_assert(NEARID_ITERS % 2 == 0, "the last step writes R and Rinv");
+  for (int it = 0; it < NEARID_ITERS; ++it) {
+    // ping-pong: odd steps write the work pair, even steps the output pair
+    const double* xi = (it & 1) ? wX : R;
+    const double* zi = (it & 1) ? wZ : Rinv;
+    double* xo = (it & 1) ? R : wX;
+    double* zo = (it & 1) ? Rinv : wZ;
+    nearid_kernel<<<n, TW * 32, smem, stream>>>(n, G, ldg, xi, zi, ld, xo, zo, it, alt, emax);
+  }
+  hq_count_launches(NEARID_ITERS);
+  return (int)cudaGetLastError();
+}
+
 extern "C" int hq_tri(cudaStream_t stream, int n, int mode, const double* A, int lda,
-                      const double* B, int ldb, const double* rs, double* X, int ldx) {
-  return hq_tri2(stream, n, mode, A, lda, B, ldb, rs, X, ldx, -1, nullptr, 0, nullptr, 0,
-                 nullptr, nullptr, 0);
+                      const double* B, int ldb, const double* rs, double* X, int ldx,
+                      const int* gate) {
+  return hq_tri2g(stream, n, mode, A, lda, B, ldb, rs, X, ldx, -1, nullptr, 0, nullptr, 0,
+                  nullptr, nullptr, 0, gate);
 }
 
 extern "C" int hq_tri2(cudaStream_t stream, int n, int mode0, const double* A0, int lda0,
                        const double* B0, int ldb0, const double* rs0, double* X0, int ldx0,
                        int mode1, const double* A1, int lda1, const double* B1, int ldb1,
                        const double* rs1, double* X1, int ldx1) {
+  return hq_tri2g(stream, n, mode0, A0, lda0, B0, ldb0, rs0, X0, ldx0, mode1, A1, lda1, B1, ldb1,
+                  rs1, X1, ldx1, nullptr);
+}
+
+extern "C" int hq_tri2g(cudaStream_t stream, int n, int mode0, const double* A0, int lda0,
+                        const double* B0, int ldb0, const double* rs0, double* X0, int ldx0,
+                        int mode1, const double* A1, int lda1, const double* B1, int ldb1,
+                        const double* rs1, double* X1, int ldx1, const int* gate) {
   if (n <= 0) return 0;
   if (n > GN || mode0 < 0 || mode0 > 1 || mode1 < -1 || mode1 > 1)
     return (int)cudaErrorInvalidValue;
@@ -611,7 +763,7 @@ extern "C" int hq_tri2(cudaStream_t stream, int n, int mode0, const double* A0, 
   if (e != cudaSuccess) return (int)e;
   const TriJob j0 = {mode0, A0, lda0, B0, ldb0, rs0, X0, ldx0};
   const TriJob j1 = {mode1 < 0 ? 0 : mode1, A1, lda1, B1, ldb1, rs1, X1, ldx1};
-  tri_kernel<<<mode1 < 0 ? n : 2 * n, TW * 32, smem, stream>>>(n, j0, j1);
+  tri_kernel<<<mode1 < 0 ? n : 2 * n, TW * 32, smem, stream>>>(n, j0, j1, gate);
   hq_count_launches(1);
   return (int)cudaGetLastError();
 }
