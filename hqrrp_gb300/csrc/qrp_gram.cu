@@ -76,7 +76,8 @@ static_assert(OWN == 2 * CLW, "each warp of a cluster CTA updates two own column
 // largest; the lowest index among residuals equal to 2^-15), the warp holding column p publishes
 // l = S[:, p] / sqrt(S[p][p]) over the active rows (0 elsewhere), and every
 // thread updates its entries by S_ij -= l_i l_j -- a no-op on eliminated
-// rows and columns, so the update needs no masks.  Three barriers per step.
+// rows and columns, so the update needs no masks.  Every warp finds the
+// pivot itself (one warp maximum), so a step takes two barriers.
 // Writes perm[k] (source column of position k) and R = Rs diag(sqrt(G_pp))
 // in FP64 (upper, zeros below), Rs the scaled factor; *stat = 0, or `bit`
 // with R = I and perm = identity when a scaled pivot is not above
@@ -89,7 +90,7 @@ __global__ void __launch_bounds__(CT, 1)
   extern __shared__ float s_Rp[];  // GN * GN: s_Rp[k * GN + i] = row k of Rs at source column i
   __shared__ double s_sc[GN], s_rt[GN];
   __shared__ float s_key[GN], s_d[GN], s_l[GN], s_r[GN], s_wmax[CW];
-  __shared__ int s_ord[GN], s_act[GN], s_bad;
+  __shared__ int s_ord[GN];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   static_assert(CT == 512 && GN == 128, "register layout: 16 warps x 32 lanes, 4 x 8 entries");
   for (int j = tid; j < GN; j += CT) {
@@ -100,7 +101,6 @@ __global__ void __launch_bounds__(CT, 1)
     s_rt[j] = rt;
     s_sc[j] = ok ? 1.0 / rt : 0.0;
     s_key[j] = ok ? (float)log2(d) : -4096.0f;  // squared norm, scaled below
-    s_act[j] = j < n;
   }
   __syncthreads();
   if (warp == 0) {
@@ -132,45 +132,60 @@ __global__ void __launch_bounds__(CT, 1)
   }
   __syncthreads();
 
+  // Per lane: the keys and active flags of columns lane + 32 q.
+  float keyr[4];
+  int actr[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int j = lane + 32 * q;
+    keyr[q] = j < n ? s_key[j] : 0.0f;
+    actr[q] = j < n;
+  }
   int fail = 0;
   for (int k = 0; k < n; ++k) {
-    // Warp 0: the pivot and its scalars.  One 32-bit key per column: the
-    // residual's FP32 bits above the low 8 (positive floats order like their
-    // bits) and 255 - j below them, so one warp maximum gives the largest
-    // residual and, among residuals equal to 2^-15, the lowest column; 0 =
-    // no active column.
-    if (warp == 0) {
-      unsigned best = 0u;
+    // Every warp finds the pivot: one 32-bit key per column, the residual's
+    // FP32 bits above the low 8 (positive floats order like their bits) and
+    // 255 - j below them, so one warp maximum gives the largest residual
+    // and, among residuals equal to 2^-15, the lowest column.
+    float dq[4];
+    unsigned best = 0u;
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int j = lane + 32 * q;
-        if (j < n && s_act[j]) {
-          const float v = s_key[j] * s_d[j];
-          const unsigned vb = v > 0.0f ? __float_as_uint(v) : 0u;  // NaN and v <= 0: lowest
-          best = max(best, (vb & ~255u) | (unsigned)(255 - j));
-        }
-      }
-      best = __reduce_max_sync(0xffffffffu, best);
-      const int bp = best ? 255 - (int)(best & 255u) : n;
-      if (lane == 0) {
-        const float d = bp < n ? s_d[bp] : 0.0f;
-        const int bad = !(d > PIVOT32_REL_MIN);  // also NaN and a zero column
-        s_bad = bad;
-        s_r[k] = bad ? 1.0f : sqrtf(d);
-        s_ord[k] = bp < n ? bp : 0;
-        if (bp < n) s_act[bp] = 0;
+    for (int q = 0; q < 4; ++q) {
+      const int j = lane + 32 * q;
+      dq[q] = s_d[j];
+      if (actr[q]) {
+        const float v = keyr[q] * dq[q];
+        const unsigned vb = v > 0.0f ? __float_as_uint(v) : 0u;  // NaN and v <= 0: lowest
+        best = max(best, (vb & ~255u) | (unsigned)(255 - j));
       }
     }
-    __syncthreads();
-    if (s_bad) {
+    best = __reduce_max_sync(0xffffffffu, best);
+    const int p = best ? 255 - (int)(best & 255u) : 0;
+    const int pq = p >> 5;
+    float dsel = dq[0];
+#pragma unroll
+    for (int q = 1; q < 4; ++q)
+      if (q == pq) dsel = dq[q];
+    const float dp = __shfl_sync(0xffffffffu, dsel, p & 31);
+    if (best == 0u || !(dp > PIVOT32_REL_MIN)) {  // also NaN and a zero column
       fail = 1;
       break;
     }
-    const int p = s_ord[k];
-    // The warp holding column p publishes l over the active rows.
+    if ((p & 31) == lane) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (q == pq) actr[q] = 0;
+    }
+    const float r = sqrtf(dp);
+    if (tid == 0) {
+      s_r[k] = r;
+      s_ord[k] = p;
+    }
+    // The warp holding column p publishes l over the active rows (row
+    // lane + 32 a is this lane's column slot a: its flag is actr[a]).
     if (warp == (p & 15)) {
       const int cp = p >> 4;
-      const float rinv = 1.0f / s_r[k];
+      const float rinv = 1.0f / r;
 #pragma unroll
       for (int a = 0; a < 4; ++a) {
         float v = S[a][0];
@@ -178,7 +193,7 @@ __global__ void __launch_bounds__(CT, 1)
         for (int c = 1; c < 8; ++c)
           if (c == cp) v = S[a][c];
         const int i = lane + 32 * a;
-        const float l = (i < n && s_act[i]) ? v * rinv : 0.0f;
+        const float l = actr[a] ? v * rinv : 0.0f;
         s_l[i] = l;
         s_Rp[k * GN + i] = l;
       }
@@ -302,10 +317,11 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CLT, 1)
   for (int c = tid; c < nown; c += CLT) s_d0[c] = Xc[(rank + CL * c) + c * LDS];
 
   // Publish own column kk (local c): scalars, final diagonal, scaled rows
-  // below it, into every CTA's buffers of parity par.
+  // below it, into every CTA's buffers of parity par.  Thread 0 wrote the
+  // column's diagonal entry itself (it updates row kk), so it takes the
+  // scalars before the barrier that orders the other rows' updates.
   auto publish = [&](int kk, int par) {
     const int c = kk / CL;
-    __syncthreads();
     if (tid == 0) {
       cluster_scalars(mode, Xc[kk + c * LDS], s_d0[c], s_pub);
       Xc[kk + c * LDS] = s_pub[0];
