@@ -159,14 +159,23 @@ int hq_permute_cols(cudaStream_t stream, int rows, double* X, int ldx, int nc, c
                     double* tmp, int* labels, int* label_tmp);
 
 /* ---- Split-BF16 (Ozaki) FP64 products on tcgen05 -------------------------
- * side 0 = M side (128-row tiles), 1 = N side (64-row tiles).  X element
+ * side 0 = M side (128-row tiles), 1 = N side (80-row tiles).  X element
  * (r, k) at X[r*rs + k*ks]; tiles sized by hq_ozk_tile_bytes; exps needs
  * rows rounded up to the tile height.  gemm: mode 0 writes sign * X Y^T to C,
  * mode 1 adds it; C element (r, c) at C[r*crs + c*ccs]; ws (optional) holds
  * split-K slices for mode 0. */
 size_t hq_ozk_tile_bytes(int rows, int K, int S, int side);
+/* raw (may be NULL): rows_total ints of scratch; when given, the two-pass
+ * split of few long rows takes its row maxima with several CTAs per row. */
 int hq_ozk_split(cudaStream_t stream, const double* X, long long rs, long long ks, int R, int K,
-                 int S, int side, void* tiles, int* exps);
+                 int S, int side, void* tiles, int* exps, int* raw);
+/* Rows rounded up to the tile height of a side. */
+int hq_ozk_split_rows(int R, int side);
+/* raw[r] := largest FP64 exponent field of row r (r < R; 0 up to rows_total),
+ * several CTAs per row: the row maxima hq_ozk_split_raw takes, computed once
+ * when both operands of a product are the same matrix. */
+int hq_ozk_rowmax_raw(cudaStream_t stream, const double* X, long long rs, long long ks, int R,
+                      int K, int rows_total, int* raw);
 /* The same split (S = 7) from each row's largest FP64 exponent field raw[r]
  * (rows < R), computed elsewhere: one streaming pass. */
 int hq_ozk_split_raw(cudaStream_t stream, const double* X, long long rs, long long ks, int R,

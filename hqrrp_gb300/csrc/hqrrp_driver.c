@@ -193,6 +193,7 @@ typedef struct {
   int dq_nb;      /* the HQRRP block size dgeqp4 uses in this call */
   void *ozA, *ozB; /* digit tiles of the two operands of a mixed product */
   int *ozea, *ozeb;
+  int* ozraw; /* row maxima scratch of the splits (exponent fields) */
   /* Mixed mode: per global column, the largest FP64 exponent field of the
    * trailing matrix below the next block's diagonal, written by the epilogue
    * of the update that produced it (and permuted with the columns), so the
@@ -457,6 +458,7 @@ static int ws_setup(hq_ws* w, int m, int n, int nb, int pp, int pw) {
     w->ozB = ws_alloc(w, b);
     w->ozea = ws_alloc(w, sizeof(int) * (size_t)rows);
     w->ozeb = ws_alloc(w, sizeof(int) * (size_t)rows);
+    w->ozraw = ws_alloc(w, sizeof(int) * (size_t)rows);
     w->colexp = ws_alloc(w, sizeof(int) * (size_t)(imax(n, 1) + 64));
     w->ozUT = ws_alloc(w, hq_ozk_tile_bytes(kmax, m, S, 0));
     w->ozU = ws_alloc(w, hq_ozk_tile_bytes(m, kmax, S, 0));
@@ -530,11 +532,22 @@ static int ozk_product_x(hq_ws* w, int S, int M, int N, int K, const double* X, 
   const void* at = xt ? xt : w->ozA;
   const int* ae = xt ? xe : w->ozea;
   const int ovr = w->ph_override;
-  if (!xt) CK(hq_ozk_split(w->st, X, xrs, xks, M, K, S, 0, w->ozA, w->ozea));
-  if (y_raw)
-    CK(hq_ozk_split_raw(w->st, Y, yrs, yks, N, K, S, short_k ? 2 : 1, w->ozB, w->ozeb, y_raw));
-  else
-    CK(hq_ozk_split(w->st, Y, yrs, yks, N, K, S, short_k ? 2 : 1, w->ozB, w->ozeb));
+  const int yside = short_k ? 2 : 1;
+  if (!xt && !y_raw && X == Y && xrs == yrs && xks == yks && M == N && S == OZK_SLICES &&
+      K >= 512 && w->ozraw) {
+    /* A Gram product (both operands the same matrix): one pass of row maxima
+     * for both splits. */
+    const int rt = imax(hq_ozk_split_rows(M, 0), hq_ozk_split_rows(N, yside));
+    CK(hq_ozk_rowmax_raw(w->st, X, xrs, xks, M, K, rt, w->ozraw));
+    CK(hq_ozk_split_raw(w->st, X, xrs, xks, M, K, S, 0, w->ozA, w->ozea, w->ozraw));
+    CK(hq_ozk_split_raw(w->st, Y, yrs, yks, N, K, S, yside, w->ozB, w->ozeb, w->ozraw));
+  } else {
+    if (!xt) CK(hq_ozk_split(w->st, X, xrs, xks, M, K, S, 0, w->ozA, w->ozea, w->ozraw));
+    if (y_raw)
+      CK(hq_ozk_split_raw(w->st, Y, yrs, yks, N, K, S, yside, w->ozB, w->ozeb, y_raw));
+    else
+      CK(hq_ozk_split(w->st, Y, yrs, yks, N, K, S, yside, w->ozB, w->ozeb, w->ozraw));
+  }
   prof_mark(w, ovr >= 0 ? ovr : PH_SPLIT, 0.0);
   if (short_k)
     CK(hq_ozk_gemm_short(w->st, &w->ds->dev, M, N, K, S, at, ae, w->ozB, w->ozeb, mode, sign, Cm,
@@ -561,8 +574,8 @@ static int ozk_product(hq_ws* w, int S, int M, int N, int K, const double* X, lo
 /* Split U' (mp x b, w->U) once for the block: as U'^T (b rows, K = mp) and
  * as U' (mp rows, K = b), both M-side digit tiles. */
 static int split_block_u(hq_ws* w, int mp, int b) {
-  CK(hq_ozk_split(w->st, w->U, w->ldu, 1, b, mp, OZK_SLICES, 0, w->ozUT, w->ozUTe));
-  CK(hq_ozk_split(w->st, w->U, 1, w->ldu, mp, b, OZK_SLICES, 0, w->ozU, w->ozUe));
+  CK(hq_ozk_split(w->st, w->U, w->ldu, 1, b, mp, OZK_SLICES, 0, w->ozUT, w->ozUTe, w->ozraw));
+  CK(hq_ozk_split(w->st, w->U, 1, w->ldu, mp, b, OZK_SLICES, 0, w->ozU, w->ozUe, w->ozraw));
   prof_mark(w, PH_SPLIT, 0.0);
   return HQ_OK;
 }

@@ -171,6 +171,115 @@ __global__ void ozk_split_kernel(const double* __restrict__ X, long long rs, lon
   }
 }
 
+// Column-major operand with short rows (row stride 1, K <= CM_KMAX, e.g. a
+// panel's rows with K = its columns): reading a row walks a column stride
+// per entry, so a CTA first stages 32 consecutive rows x K in shared memory
+// with coalesced loads (one warp load = 32 consecutive rows of one column),
+// then splits each row exactly as ozk_split_kernel does (same digits and
+// exponents), one warp per row.
+constexpr int CM_KMAX = 128;
+template <int S>
+__global__ void __launch_bounds__(256) ozk_split_cm_kernel(const double* __restrict__ X,
+                                                           long long ks, int R, int K, int KB,
+                                                           int rows_total,
+                                                           uint8_t* __restrict__ tiles,
+                                                           int* __restrict__ exps) {
+  constexpr unsigned long long BIAS = 0x8080808080808080ULL >> (8 * (8 - S));
+  __shared__ double tile[CM_KMAX][33];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nchunk = KB * (TK / 8);
+  const long long kp = (long long)KB * TK;
+  const long long slice_bytes = (long long)rows_total * kp * 2;
+  const int r0 = blockIdx.x * 32;
+  for (int k = warp; k < K; k += 8) {
+    const int r = r0 + lane;
+    tile[k][lane] = r < R ? X[(long long)r + (long long)k * ks] : 0.0;
+  }
+  __syncthreads();
+  for (int rr = warp; rr < 32; rr += 8) {
+    const int r = r0 + rr;
+    if (r >= rows_total) break;
+    const bool live = r < R;
+    long long mb = 0;
+    if (live)
+      for (int k = lane; k < K; k += 32) {
+        const long long bb = __double_as_longlong(tile[k][rr]) & 0x7FFFFFFFFFFFFFFFLL;
+        mb = bb > mb ? bb : mb;
+      }
+    for (int o = 16; o > 0; o >>= 1) {
+      const long long ob = __shfl_xor_sync(0xffffffffu, mb, o);
+      mb = ob > mb ? ob : mb;
+    }
+    const int bexp = (int)(mb >> 52);
+    const int e = bexp == 0 ? 0 : bexp - 1022;
+    if (lane == 0) exps[r] = e;
+    const int shift_base = 8 * S - 1076 - e;
+    for (int ch = lane; ch < nchunk; ch += 32) {
+      const int k0 = ch * 8;
+      unsigned long long W[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const long long V = (live && k0 + j < K) ? fixed_point(tile[k0 + j][rr], shift_base) : 0;
+        W[j] = (unsigned long long)V + BIAS;
+      }
+      uint8_t* base = tiles + ((long long)r * kp + k0) * 2;
+#pragma unroll
+      for (int s = 0; s < S; ++s) {
+        const int p = S - 1 - s;
+        uint32_t w[4];
+#pragma unroll
+        for (int j = 0; j < 8; j += 2) {
+          uint32_t u0, u1;
+          if (p == S - 1) {
+            u0 = (uint32_t)(W[j] >> (8 * p));
+            u1 = (uint32_t)(W[j + 1] >> (8 * p));
+          } else {
+            u0 = (uint32_t)(W[j] >> (8 * p)) & 255u;
+            u1 = (uint32_t)(W[j + 1] >> (8 * p)) & 255u;
+          }
+          w[j >> 1] = __byte_perm(digit_scaled(u0, s), digit_scaled(u1, s), 0x7632);
+        }
+        *reinterpret_cast<uint4*>(base + (long long)s * slice_bytes) =
+            make_uint4(w[0], w[1], w[2], w[3]);
+      }
+    }
+  }
+}
+
+// Largest exponent field of each row, several CTAs per row (ROWMAX_SPAN
+// entries each, eight loads in flight per thread) raising raw[r] -- zeroed
+// before -- with an integer atomicMax: the first pass of the two-pass split
+// for few long rows, which one CTA per row left latency-bound.
+constexpr int ROWMAX_SPAN = 2048;
+__global__ void __launch_bounds__(256) ozk_rowmax_atomic_kernel(const double* __restrict__ X,
+                                                                long long rs, long long ks, int K,
+                                                                int* __restrict__ raw) {
+  __shared__ long long s_max[8];
+  const int r = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int k0 = blockIdx.y * ROWMAX_SPAN;
+  const double* xr = X + (long long)r * rs;
+  long long v[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int k = k0 + tid + 256 * i;
+    v[i] = k < K ? (__double_as_longlong(xr[(long long)k * ks]) & 0x7FFFFFFFFFFFFFFFLL) : 0;
+  }
+  long long mb = 0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) mb = v[i] > mb ? v[i] : mb;
+  for (int o = 16; o > 0; o >>= 1) {
+    const long long ob = __shfl_xor_sync(0xffffffffu, mb, o);
+    mb = ob > mb ? ob : mb;
+  }
+  if (lane == 0) s_max[warp] = mb;
+  __syncthreads();
+  if (tid == 0) {
+    for (int w = 1; w < 8; ++w) mb = s_max[w] > mb ? s_max[w] : mb;
+    mb = s_max[0] > mb ? s_max[0] : mb;
+    if (mb != 0) atomicMax(raw + r, (int)(mb >> 52));
+  }
+}
+
 // One-pass variant for long rows (4096 <= K <= 16384 with 512 threads): one
 // CTA per row holds the row in registers (CPT chunks of 8 per thread), takes
 // the block maximum and writes the digits, so every entry is read from
@@ -453,20 +562,6 @@ __device__ __forceinline__ void mma_commit(uint64_t* b) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                    smem_u32(b))
                : "memory");
-}
-
-// 8 consecutive TMEM columns of this warp's 32 lanes.
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
-  uint32_t r[8];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
-      "tcgen05.wait::ld.sync.aligned;"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7])
-      : "r"(taddr)
-      : "memory");
-#pragma unroll
-  for (int j = 0; j < 8; ++j) v[j] = __uint_as_float(r[j]);
 }
 
 // (hi, lo) += x in FP32 pairs (TwoSum, then renormalise).
@@ -1202,8 +1297,24 @@ extern "C" size_t hq_ozk_tile_bytes(int rows, int K, int S, int side) {
   return (size_t)(RT * KB * S) * (size_t)(TR * TK * 2);
 }
 
+extern "C" int hq_ozk_rowmax_raw(cudaStream_t stream, const double* X, long long rs,
+                                 long long ks, int R, int K, int rows_total, int* raw) {
+  if (R <= 0 || K <= 0) return 0;
+  cudaError_t e = cudaMemsetAsync(raw, 0, sizeof(int) * (size_t)rows_total, stream);
+  if (e != cudaSuccess) return (int)e;
+  ozk_rowmax_atomic_kernel<<<dim3(R, (K + ROWMAX_SPAN - 1) / ROWMAX_SPAN), 256, 0, stream>>>(
+      X, rs, ks, K, raw);
+  hq_count_launches(1);
+  return (int)cudaGetLastError();
+}
+
+extern "C" int hq_ozk_split_rows(int R, int side) {
+  const int TR = side == 0 ? TM : (side == 2 ? TN_SHORT : TN);
+  return (R + TR - 1) / TR * TR;
+}
+
 extern "C" int hq_ozk_split(cudaStream_t stream, const double* X, long long rs, long long ks,
-                            int R, int K, int S, int side, void* tiles, int* exps) {
+                            int R, int K, int S, int side, void* tiles, int* exps, int* raw) {
   if (R <= 0 || K <= 0) return 0;
   if (S < 1 || S > 7) return (int)cudaErrorInvalidValue;
   const int TR = side == 0 ? TM : (side == 2 ? TN_SHORT : TN);
@@ -1219,14 +1330,36 @@ extern "C" int hq_ozk_split(cudaStream_t stream, const double* X, long long rs, 
   // spreads every row over CTAs.
   constexpr int FEW_ROWS = 8 * 152;
   if (S == 7 && (K > 512 * 8 * ROW_CPT || (K >= 512 && rows_total < FEW_ROWS))) {
-    int mblocks = rows_total < 8192 ? rows_total : 8192;
-    ozk_rowmax_kernel<<<mblocks, 256, 0, stream>>>(X, rs, ks, R, K, rows_total, exps);
     const long long chunks = (long long)rows_total * KB * (TK / 8);
     long long cblocks = (chunks + 255) / 256;
     if (cblocks > 65536) cblocks = 65536;
+    if (raw != nullptr) {  // row maxima with several CTAs per row (scratch given)
+      const int e = hq_ozk_rowmax_raw(stream, X, rs, ks, R, K, rows_total, raw);
+      if (e) return e;
+      ozk_split_chunk_kernel<7><<<(unsigned)cblocks, 256, 0, stream>>>(X, rs, ks, R, K, KB,
+                                                                        rows_total, t, exps, raw);
+      hq_count_launches(1);
+      return (int)cudaGetLastError();
+    }
+    int mblocks = rows_total < 8192 ? rows_total : 8192;
+    ozk_rowmax_kernel<<<mblocks, 256, 0, stream>>>(X, rs, ks, R, K, rows_total, exps);
     ozk_split_chunk_kernel<7><<<(unsigned)cblocks, 256, 0, stream>>>(X, rs, ks, R, K, KB,
                                                                       rows_total, t, exps, nullptr);
     hq_count_launches(2);
+    return (int)cudaGetLastError();
+  }
+  if (rs == 1 && ks != 1 && K <= CM_KMAX) {  // column-major rows of a short operand
+    const int cb = (rows_total + 31) / 32;
+    switch (S) {
+#define HQ_SPLIT_CM_CASE(SS)                                                            \
+  case SS:                                                                              \
+    ozk_split_cm_kernel<SS><<<cb, 256, 0, stream>>>(X, ks, R, K, KB, rows_total, t, exps); \
+    break;
+      HQ_SPLIT_CM_CASE(1) HQ_SPLIT_CM_CASE(2) HQ_SPLIT_CM_CASE(3) HQ_SPLIT_CM_CASE(4)
+      HQ_SPLIT_CM_CASE(5) HQ_SPLIT_CM_CASE(6) HQ_SPLIT_CM_CASE(7)
+#undef HQ_SPLIT_CM_CASE
+    }
+    hq_count_launches(1);
     return (int)cudaGetLastError();
   }
   if (K >= 4096 && K <= 512 * 8 * ROW_CPT && S == 7) {
