@@ -37,7 +37,12 @@ enum {
 
 #define DGEQP4_SMALL_DGEQP3 1000 /* ...var4.c:58 */
 #define DGEQP4_NB 64 /* HQRRP block size and oversampling dgeqp4 uses (...var4.c:264) */
-static int g_dgeqp4_nb = DGEQP4_NB; /* hqrrp_gb300_set_dgeqp4_block */
+/* The block size dgeqp4's HQRRP call uses on this GPU by default: the
+ * reference's 64 is a CPU default ("default values", ...var4.c:255-256); at
+ * 64 the rank-64 trailing updates are bound by the split-BF16 products' FP64
+ * epilogue, which 128 halves per output. */
+#define DGEQP4_GPU_NB 128
+static int g_dgeqp4_nb = DGEQP4_GPU_NB; /* hqrrp_gb300_set_dgeqp4_block */
 #define DGEQP4_PP 10
 #define LAPACK_NB_DGEQRF 32 /* ILAENV(1, 'DGEQRF') of reference LAPACK */
 #define LAPACK_NX_DGEQRF 128 /* ILAENV(3, 'DGEQRF'): blocked-code crossover */

@@ -70,14 +70,16 @@ int NoFLA_HQRRP_WY_blk_var4(int m_A, int n_A, double* buff_A, int ldim_A, int* b
 int hqrrp_gb300_set_precision(int mode);
 
 /* Block size of the HQRRP call inside dgeqp4 (and dgeqp4_device), with
- * oversampling 10.  The default, 64, is the reference's (...var4.c:264),
- * chosen for CPUs.  On this GPU 128 runs the 16384^2 factorization about 1.4x
- * faster.  With nb = 64, the block update's products have only 64 of their
- * 128-row tiles' rows, and the rank-64 trailing update is bound by its FP64
- * epilogue instead of its tensor-core work.  dgeqp4 with an explicit sketch
- * (hqrrp_gb300_dgeqp4_sketch) always uses 64, the reference's block
- * structure.  Returns the previous value, or -1 if nb is outside
- * 1..246. */
+ * oversampling 10.  The default is 128: the reference's 64
+ * (NoFLA_HQRRP_WY_blk_var4.c:255-264, its "default values") is a CPU choice,
+ * and on this GPU 128 runs the 16384^2 factorization about 1.5x faster.
+ * With nb = 64 the block update's products have only 64 of their 128-row
+ * tiles' rows, and the rank-64 trailing update is bound by its FP64 epilogue
+ * instead of its tensor-core work.  The block size sets the block structure
+ * of the randomized pivoting, not the interface or the output's form.
+ * dgeqp4 with an explicit sketch (hqrrp_gb300_dgeqp4_sketch) always uses 64,
+ * the reference's block structure.  Returns the previous value, or -1 if nb
+ * is outside 1..246. */
 int hqrrp_gb300_set_dgeqp4_block(int nb);
 
 /* Seed of the device Philox sketch used when no sketch is supplied. */

@@ -114,9 +114,9 @@ def test_no_gpu_error_codes(hq):
 def test_dgeqp4_block_setter(hq):
     """Host-side state only: the previous value comes back, invalid sizes are
     refused and leave it unchanged."""
-    assert hq.set_dgeqp4_block(128) == 64
+    assert hq.set_dgeqp4_block(64) == 128  # the GPU default
     with pytest.raises(ValueError):
         hq.set_dgeqp4_block(0)
     with pytest.raises(ValueError):
         hq.set_dgeqp4_block(247)
-    assert hq.set_dgeqp4_block(64) == 128
+    assert hq.set_dgeqp4_block(128) == 64

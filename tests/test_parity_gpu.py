@@ -319,15 +319,17 @@ def test_dgeqp4_rows_above_follow_hqrrp_bit_exact(hq, oracle_lib):
     assert_parity((Ag, jg, tg), (Ao, jo, to))
 
 
-def test_dgeqp4_gpu_block_size(hq, oracle_lib):
-    """dgeqp4 with HQRRP block 128 (hqrrp_gb300_set_dgeqp4_block): a different
-    block structure, so its own pivots, but the same quality, fixed columns
-    still first, and an explicit reference sketch still gets the reference's
-    block size 64 (parity with the oracle unchanged)."""
+@pytest.mark.parametrize("nb", [128, 64])
+def test_dgeqp4_block_size(hq, oracle_lib, nb):
+    """dgeqp4 with HQRRP block 128 (the GPU default) and 64 (the reference's,
+    through hqrrp_gb300_set_dgeqp4_block): each block structure has its own
+    pivots but the same quality, fixed columns still first, and an explicit
+    reference sketch still gets the reference's block size 64 (parity with the
+    oracle unchanged)."""
     m, n = 1500, 1400
     A = oracle.gaussian(m, n, 47)
     jp = _fixed_marks(n, 11)
-    prev = hq.set_dgeqp4_block(128)
+    prev = hq.set_dgeqp4_block(nb)
     try:
         Af, jpv, tau, info, _ = hq.dgeqp4(A, jp)
         G = oracle_lib.sketch(74, m - _nfix(jp, m))
