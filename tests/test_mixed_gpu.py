@@ -3,7 +3,7 @@
 Tolerances (stated here, checked per element or normwise):
 * hqrrp_gb300_ozaki_dgemm with s digits: |C - AB| <= tol(s) * (|A| |B|) per
   element, tol(6) = 2^-42, tol(7) = 2^-49 (design accuracy 2^-45 / 2^-52).
-* mixed HQRRP (the benchmark spec): ||AP - QR||_F / ||A||_F <= 1e-13 and
+* mixed HQRRP (the mixed form's target): ||AP - QR||_F / ||A||_F <= 1e-13 and
   |R_kk| / sigma_k within a factor 2 of the plain FP64 path.
 """
 import numpy as np

@@ -2,8 +2,8 @@
 
 The oracle is the CPU restatement of the reference, itself pinned to the
 reference by tests/test_oracle.py.  Both runs use the same sketch G (the
-reference's own rand()-based one, passed explicitly to the GPU).  The bar
-(the benchmark spec): jpvt identical; tau and R within 1e-12 relative.  The
+reference's own rand()-based one, passed explicitly to the GPU).  The parity bar
+for the plain path: jpvt identical; tau and R within 1e-12 relative.  The
 Householder vectors below the diagonal are compared at the same tolerance.
 """
 import numpy as np
