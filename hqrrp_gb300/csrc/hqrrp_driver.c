@@ -412,7 +412,7 @@ static int ws_setup(hq_ws* w, int m, int n, int nb, int pp, int pw) {
   w->ldw = imax(kmax, 1);
   w->ldt = imax(kmax, 1);
   w->ldz = imax(kmax, 1);
-  w->ws_elems = (size_t)8 << 20;
+  w->ws_elems = (size_t)16 << 20; /* split-K slices: 128 MB */
   size_t pe = hq_skinny_part_elems(dev, imin(imax(mY, 1), HQ_MAX_MY));
   size_t pe2 = hq_panel_part_elems(dev, imin(imax(kmax, 1), HQ_MAX_PANEL));
   w->part_elems = pe > pe2 ? pe : pe2;
