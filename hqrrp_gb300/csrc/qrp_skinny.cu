@@ -641,7 +641,14 @@ extern "C" int hq_skinny_qrp(cudaStream_t stream, const hq_device_info* dev, int
   a.bar = bar;
   a.err = err;
   a.spin_limit = spin_limit;
-  const int P = skinny_grid(dev, N);
+  // The register kernel holds up to NT / 2 columns per CTA; with as few CTAs
+  // as that allows, each stage's grid barrier has fewer arrivals to wait for
+  // (the per-column arithmetic, and so the pivots, do not depend on the
+  // partition).  The shared-memory kernel keeps one CTA per 16 columns up to
+  // one per SM.
+  const int p_reg = (N + NT / 2 - 1) / (NT / 2);
+  const bool reg_fit = mY <= 2 * 72 && p_reg <= dev->num_sms && p_reg <= 160;
+  const int P = reg_fit ? (p_reg < 1 ? 1 : p_reg) : skinny_grid(dev, N);
   if ((size_t)2 * P * a.rec > part_elems) return (int)cudaErrorInvalidValue;
   a.nloc_max = (N + P - 1) / P;
   a.ldxs = mY | 1;
