@@ -16,6 +16,7 @@ namespace {
 // U (rows x b, ldu) = unit-lower part of the reflector block stored in F.
 __global__ void unit_lower_kernel(int rows, int b, const double* __restrict__ F, int ldf,
                                   double* __restrict__ U, int ldu) {
+  HQ_PDL_WAIT();
   const long long total = (long long)rows * b;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
        e += (long long)gridDim.x * blockDim.x) {
@@ -26,6 +27,7 @@ __global__ void unit_lower_kernel(int rows, int b, const double* __restrict__ F,
 
 // E (rows x k) = [I_k; 0].
 __global__ void eye_kernel(int rows, int k, double* __restrict__ E, int lde) {
+  HQ_PDL_WAIT();
   const long long total = (long long)rows * k;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
        e += (long long)gridDim.x * blockDim.x) {
@@ -36,6 +38,7 @@ __global__ void eye_kernel(int rows, int k, double* __restrict__ E, int lde) {
 
 // X (k x k) <- copyltu(X) * sign: lower triangle kept, mirrored to the upper.
 __global__ void copyltu_kernel(int k, double* __restrict__ X, int ldx, double sign) {
+  HQ_PDL_WAIT();
   const int total = k * k;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
     const int i = e % k, j = e / k;
@@ -52,6 +55,7 @@ __global__ void copyltu_kernel(int k, double* __restrict__ X, int ldx, double si
 // at the same time, so R is served from L1 as a broadcast.
 __global__ void trsm_rt_kernel(int rows, int k, const double* __restrict__ R, int ldr,
                                double* __restrict__ Y, int ldy) {
+  HQ_PDL_WAIT();
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
     double* y = Y + r;
     for (int j = k - 1; j >= 0; --j) {
@@ -66,6 +70,7 @@ __global__ void trsm_rt_kernel(int rows, int k, const double* __restrict__ R, in
 __global__ void scatter_cols_kernel(int rows, int ncols, const double* __restrict__ src, int lds,
                                     const int* __restrict__ labels, double* __restrict__ dst,
                                     int ldd, int accumulate) {
+  HQ_PDL_WAIT();
   const long long total = (long long)rows * ncols;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
        e += (long long)gridDim.x * blockDim.x) {
@@ -81,6 +86,7 @@ __global__ void scatter_cols_kernel(int rows, int ncols, const double* __restric
 __global__ void rk_unpermute_kernel(int k, int n, const double* __restrict__ F, int ldf,
                                     const int* __restrict__ labels, double* __restrict__ M,
                                     int ldm) {
+  HQ_PDL_WAIT();
   const long long total = (long long)k * n;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
        e += (long long)gridDim.x * blockDim.x) {
@@ -92,6 +98,7 @@ __global__ void rk_unpermute_kernel(int k, int n, const double* __restrict__ F, 
 // dst (rows x cols) += alpha * src.
 __global__ void add_matrix_kernel(int rows, int cols, double alpha, const double* __restrict__ src,
                                   int lds, double* __restrict__ dst, int ldd) {
+  HQ_PDL_WAIT();
   const long long total = (long long)rows * cols;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
        e += (long long)gridDim.x * blockDim.x) {
@@ -102,6 +109,7 @@ __global__ void add_matrix_kernel(int rows, int cols, double alpha, const double
 
 // A[i, i] = v for i < n.
 __global__ void set_diag_kernel(int n, double* __restrict__ A, int lda, double v) {
+  HQ_PDL_WAIT();
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     A[i + (long long)i * lda] = v;
 }
@@ -111,6 +119,7 @@ __global__ void set_diag_kernel(int n, double* __restrict__ A, int lda, double v
 // unit diagonal, U^T U = U'^T U' + L + L^T + I.
 __global__ void gram_unit_fix_kernel(int b, const double* __restrict__ Up, int ldu,
                                      double* __restrict__ Z, int ldz) {
+  HQ_PDL_WAIT();
   const int total = b * b;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
     const int r = e % b, c = e / b;
@@ -130,21 +139,21 @@ inline unsigned grid_for(long long total) {
 extern "C" int hq_unit_lower(cudaStream_t st, int rows, int b, const double* F, int ldf, double* U,
                              int ldu) {
   if (rows <= 0 || b <= 0) return 0;
-  unit_lower_kernel<<<grid_for((long long)rows * b), 256, 0, st>>>(rows, b, F, ldf, U, ldu);
+  hq_launch(unit_lower_kernel, grid_for((long long)rows * b), 256, 0, st, rows, b, F, ldf, U, ldu);
   hq_count_launches(1);
   return (int)cudaGetLastError();
 }
 
 extern "C" int hq_eye(cudaStream_t st, int rows, int k, double* E, int lde) {
   if (rows <= 0 || k <= 0) return 0;
-  eye_kernel<<<grid_for((long long)rows * k), 256, 0, st>>>(rows, k, E, lde);
+  hq_launch(eye_kernel, grid_for((long long)rows * k), 256, 0, st, rows, k, E, lde);
   hq_count_launches(1);
   return (int)cudaGetLastError();
 }
 
 extern "C" int hq_copyltu(cudaStream_t st, int k, double* X, int ldx, double sign) {
   if (k <= 0) return 0;
-  copyltu_kernel<<<grid_for((long long)k * k), 256, 0, st>>>(k, X, ldx, sign);
+  hq_launch(copyltu_kernel, grid_for((long long)k * k), 256, 0, st, k, X, ldx, sign);
   hq_count_launches(1);
   return (int)cudaGetLastError();
 }
@@ -153,7 +162,7 @@ extern "C" int hq_trsm_rt(cudaStream_t st, int rows, int k, const double* R, int
                           int ldy) {
   if (rows <= 0 || k <= 0) return 0;
   const unsigned blocks = (unsigned)((rows + 63) / 64);
-  trsm_rt_kernel<<<blocks, 64, 0, st>>>(rows, k, R, ldr, Y, ldy);
+  hq_launch(trsm_rt_kernel, blocks, 64, 0, st, rows, k, R, ldr, Y, ldy);
   hq_count_launches(1);
   return (int)cudaGetLastError();
 }
@@ -161,7 +170,7 @@ extern "C" int hq_trsm_rt(cudaStream_t st, int rows, int k, const double* R, int
 extern "C" int hq_scatter_cols(cudaStream_t st, int rows, int ncols, const double* src, int lds,
                                const int* labels, double* dst, int ldd, int accumulate) {
   if (rows <= 0 || ncols <= 0) return 0;
-  scatter_cols_kernel<<<grid_for((long long)rows * ncols), 256, 0, st>>>(
+  hq_launch(scatter_cols_kernel, grid_for((long long)rows * ncols), 256, 0, st,
       rows, ncols, src, lds, labels, dst, ldd, accumulate);
   hq_count_launches(1);
   return (int)cudaGetLastError();
@@ -170,7 +179,7 @@ extern "C" int hq_scatter_cols(cudaStream_t st, int rows, int ncols, const doubl
 extern "C" int hq_rk_unpermute(cudaStream_t st, int k, int n, const double* F, int ldf,
                                const int* labels, double* M, int ldm) {
   if (k <= 0 || n <= 0) return 0;
-  rk_unpermute_kernel<<<grid_for((long long)k * n), 256, 0, st>>>(k, n, F, ldf, labels, M, ldm);
+  hq_launch(rk_unpermute_kernel, grid_for((long long)k * n), 256, 0, st, k, n, F, ldf, labels, M, ldm);
   hq_count_launches(1);
   return (int)cudaGetLastError();
 }
@@ -178,7 +187,7 @@ extern "C" int hq_rk_unpermute(cudaStream_t st, int k, int n, const double* F, i
 extern "C" int hq_add_matrix(cudaStream_t st, int rows, int cols, double alpha, const double* src,
                              int lds, double* dst, int ldd) {
   if (rows <= 0 || cols <= 0) return 0;
-  add_matrix_kernel<<<grid_for((long long)rows * cols), 256, 0, st>>>(rows, cols, alpha, src, lds,
+  hq_launch(add_matrix_kernel, grid_for((long long)rows * cols), 256, 0, st, rows, cols, alpha, src, lds,
                                                                       dst, ldd);
   hq_count_launches(1);
   return (int)cudaGetLastError();
@@ -186,7 +195,7 @@ extern "C" int hq_add_matrix(cudaStream_t st, int rows, int cols, double alpha, 
 
 extern "C" int hq_set_diag(cudaStream_t st, int n, double* A, int lda, double v) {
   if (n <= 0) return 0;
-  set_diag_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, A, lda, v);
+  hq_launch(set_diag_kernel, (n + 255) / 256, 256, 0, st, n, A, lda, v);
   hq_count_launches(1);
   return (int)cudaGetLastError();
 }
@@ -194,7 +203,7 @@ extern "C" int hq_set_diag(cudaStream_t st, int n, double* A, int lda, double v)
 extern "C" int hq_gram_unit_fix(cudaStream_t st, int b, const double* Up, int ldu, double* Z,
                                 int ldz) {
   if (b <= 0) return 0;
-  gram_unit_fix_kernel<<<grid_for((long long)b * b), 256, 0, st>>>(b, Up, ldu, Z, ldz);
+  hq_launch(gram_unit_fix_kernel, grid_for((long long)b * b), 256, 0, st, b, Up, ldu, Z, ldz);
   hq_count_launches(1);
   return (int)cudaGetLastError();
 }

@@ -20,6 +20,7 @@ __global__ void __launch_bounds__(NT, 2)
     dgemm_tile(int M, int N, int K, int kchunk, double alpha, const double* __restrict__ A,
                int lda, const double* __restrict__ B, int ldb, double beta,
                double* __restrict__ Cm, int ldc, double* __restrict__ ws) {
+  HQ_PDL_WAIT();
   __shared__ double As[BK][BM + 1];
   __shared__ double Bs[BK][BN + 1];
   const int tid = threadIdx.x;
@@ -131,6 +132,7 @@ __global__ void __launch_bounds__(NT, 2)
 __global__ void dgemm_splitk_sum(int M, int N, int splits, double alpha,
                                  const double* __restrict__ ws, double beta,
                                  double* __restrict__ Cm, int ldc) {
+  HQ_PDL_WAIT();
   const size_t total = (size_t)M * N;
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total;
        e += (size_t)gridDim.x * blockDim.x) {
@@ -143,6 +145,7 @@ __global__ void dgemm_splitk_sum(int M, int N, int splits, double alpha,
 }
 
 __global__ void dgemm_scale(int M, int N, double beta, double* __restrict__ Cm, int ldc) {
+  HQ_PDL_WAIT();
   const size_t total = (size_t)M * N;
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total;
        e += (size_t)gridDim.x * blockDim.x) {
@@ -161,7 +164,7 @@ extern "C" int hq_dgemm(cudaStream_t stream, const hq_device_info* dev, char tra
   if (M <= 0 || N <= 0) return 0;
   if (K <= 0 || alpha == 0.0) {
     if (beta == 1.0) return 0;
-    dgemm_scale<<<dev->num_sms * 4, 256, 0, stream>>>(M, N, beta, Cm, ldc);
+    hq_launch(dgemm_scale, dev->num_sms * 4, 256, 0, stream, M, N, beta, Cm, ldc);
     hq_count_launches(1);
     return (int)cudaGetLastError();
   }
@@ -188,22 +191,22 @@ extern "C" int hq_dgemm(cudaStream_t stream, const hq_device_info* dev, char tra
   dim3 grid(gm, gn, splits);
   double* out_ws = splits > 1 ? ws : nullptr;
   if (!ta && !tb)
-    dgemm_tile<false, false><<<grid, NT, 0, stream>>>(M, N, K, kchunk, alpha, A, lda, B, ldb,
+    hq_launch(dgemm_tile<false, false>, grid, NT, 0, stream, M, N, K, kchunk, alpha, A, lda, B, ldb,
                                                        beta, Cm, ldc, out_ws);
   else if (ta && !tb)
-    dgemm_tile<true, false><<<grid, NT, 0, stream>>>(M, N, K, kchunk, alpha, A, lda, B, ldb,
+    hq_launch(dgemm_tile<true, false>, grid, NT, 0, stream, M, N, K, kchunk, alpha, A, lda, B, ldb,
                                                       beta, Cm, ldc, out_ws);
   else if (!ta && tb)
-    dgemm_tile<false, true><<<grid, NT, 0, stream>>>(M, N, K, kchunk, alpha, A, lda, B, ldb,
+    hq_launch(dgemm_tile<false, true>, grid, NT, 0, stream, M, N, K, kchunk, alpha, A, lda, B, ldb,
                                                       beta, Cm, ldc, out_ws);
   else
-    dgemm_tile<true, true><<<grid, NT, 0, stream>>>(M, N, K, kchunk, alpha, A, lda, B, ldb,
+    hq_launch(dgemm_tile<true, true>, grid, NT, 0, stream, M, N, K, kchunk, alpha, A, lda, B, ldb,
                                                      beta, Cm, ldc, out_ws);
   if (splits > 1) {
     long total = (long)M * N;
     int blocks = (int)((total + 255) / 256);
     if (blocks > dev->num_sms * 8) blocks = dev->num_sms * 8;
-    dgemm_splitk_sum<<<blocks, 256, 0, stream>>>(M, N, splits, alpha, ws, beta, Cm, ldc);
+    hq_launch(dgemm_splitk_sum, blocks, 256, 0, stream, M, N, splits, alpha, ws, beta, Cm, ldc);
   }
   hq_count_launches(splits > 1 ? 2 : 1);
   return (int)cudaGetLastError();

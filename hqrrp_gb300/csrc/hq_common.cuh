@@ -12,6 +12,34 @@
 
 #define HQ_WARP 32
 
+// Launch with programmatic dependent launch.  The grid may then be scheduled
+// while the previous kernel on the stream is still finishing; every kernel
+// launched this way begins with HQ_PDL_WAIT(), which holds each thread until
+// that kernel has completed and its writes are visible.  Nothing is read or
+// written before the wait, so the stream order is kept exactly; what is saved
+// is the latency between the end of one kernel and the start of the next
+// (about 4.1 against 1.4 microseconds per launch for a chain of small
+// dependent kernels on GB300).  The wait returns at once in a grid launched
+// without the attribute (HQRRP_GB300_PDL=0).  Launch errors are left to the
+// caller's cudaGetLastError(), as with <<<>>>.
+#define HQ_PDL_WAIT() asm volatile("griddepcontrol.wait;" ::: "memory")
+
+template <typename... KArgs, typename... Args>
+static inline void hq_launch(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                             cudaStream_t stream, Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = hq_pdl() ? 1 : 0;
+  (void)cudaLaunchKernelEx(&cfg, kernel, static_cast<Args&&>(args)...);
+}
+
 __device__ __forceinline__ unsigned hq_ld_acquire(const unsigned* p) {
   unsigned v;
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");

@@ -240,6 +240,11 @@ int hq_gram_unit_fix(cudaStream_t st, int b, const double* Up, int ldu, double* 
 int hq_copy_matrix(cudaStream_t stream, int rows, int cols, const double* src, int lds,
                    double* dst, int ldd);
 
+/* Programmatic dependent launch of this library's kernels: on unless
+ * HQRRP_GB300_PDL=0 (read by each call's workspace setup). */
+void hq_set_pdl(int on);
+int hq_pdl(void);
+
 #ifdef __cplusplus
 }
 #endif

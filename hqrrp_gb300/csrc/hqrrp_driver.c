@@ -405,6 +405,10 @@ static int ws_setup(hq_ws* w, int m, int n, int nb, int pp, int pw) {
   const hq_device_info* dev = &w->ds->dev;
   const int mY = nb + pp;
   const int kmax = imax(nb, pw);
+  /* Programmatic dependent launch between this library's kernels, unless
+   * HQRRP_GB300_PDL=0. */
+  const char* pdl_env = getenv("HQRRP_GB300_PDL");
+  hq_set_pdl(!(pdl_env && pdl_env[0] == '0'));
   w->ldg = round_up(imax(mY, 1), 2);
   w->ldy = w->ldg;
   w->ldb = w->ldg;

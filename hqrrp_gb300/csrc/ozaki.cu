@@ -111,6 +111,7 @@ template <int S>
 __global__ void ozk_split_kernel(const double* __restrict__ X, long long rs, long long ks, int R,
                                  int K, int TR, int KB, int rows_total,
                                  uint8_t* __restrict__ tiles, int* __restrict__ exps) {
+  HQ_PDL_WAIT();
   constexpr unsigned long long BIAS = 0x8080808080808080ULL >> (8 * (8 - S));
   const int lane = threadIdx.x & 31;
   const int warps = blockDim.x >> 5;
@@ -184,6 +185,7 @@ __global__ void __launch_bounds__(256) ozk_split_cm_kernel(const double* __restr
                                                            int rows_total,
                                                            uint8_t* __restrict__ tiles,
                                                            int* __restrict__ exps) {
+  HQ_PDL_WAIT();
   constexpr unsigned long long BIAS = 0x8080808080808080ULL >> (8 * (8 - S));
   __shared__ double tile[CM_KMAX][33];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -254,6 +256,7 @@ constexpr int ROWMAX_SPAN = 2048;
 __global__ void __launch_bounds__(256) ozk_rowmax_atomic_kernel(const double* __restrict__ X,
                                                                 long long rs, long long ks, int K,
                                                                 int* __restrict__ raw) {
+  HQ_PDL_WAIT();
   __shared__ long long s_max[8];
   const int r = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int k0 = blockIdx.y * ROWMAX_SPAN;
@@ -289,6 +292,7 @@ template <int S, int CPT>
 __global__ void __launch_bounds__(512) ozk_split_row_kernel(
     const double* __restrict__ X, long long rs, long long ks, int R, int K, int TR, int KB,
     int rows_total, uint8_t* __restrict__ tiles, int* __restrict__ exps) {
+  HQ_PDL_WAIT();
   constexpr unsigned long long BIAS = 0x8080808080808080ULL >> (8 * (8 - S));
   constexpr int NTH = 512;
   __shared__ long long s_max[NTH / 32];
@@ -378,6 +382,7 @@ __global__ void __launch_bounds__(512) ozk_split_row_kernel(
 __global__ void __launch_bounds__(256) ozk_rowmax_kernel(const double* __restrict__ X,
                                                          long long rs, long long ks, int R, int K,
                                                          int rows_total, int* __restrict__ exps) {
+  HQ_PDL_WAIT();
   __shared__ long long s_max[8];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (int r = blockIdx.x; r < rows_total; r += gridDim.x) {
@@ -409,6 +414,7 @@ template <int S>
 __global__ void __launch_bounds__(256) ozk_split_chunk_kernel(
     const double* __restrict__ X, long long rs, long long ks, int R, int K, int KB, int rows_total,
     uint8_t* __restrict__ tiles, int* __restrict__ exps, const int* __restrict__ raw) {
+  HQ_PDL_WAIT();
   constexpr unsigned long long BIAS = 0x8080808080808080ULL >> (8 * (8 - S));
   const int nchunk = KB * (TK / 8);
   const long long kp = (long long)KB * TK;
@@ -729,6 +735,7 @@ __device__ __forceinline__ void issue_any(uint32_t tb, uint64_t da0, uint64_t db
 __global__ void __launch_bounds__(NT, 1) ozk_gemm_kernel(OzkArgs a,
                                                         const __grid_constant__ CUtensorMap tmA,
                                                         const __grid_constant__ CUtensorMap tmB) {
+  HQ_PDL_WAIT();
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   __shared__ __align__(8) uint64_t full_bar[MAX_STAGES], empty_bar[MAX_STAGES];
   __shared__ __align__(8) uint64_t drain_full, drain_empty, done_bar;
@@ -935,6 +942,7 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
 
 __global__ void __launch_bounds__(NT, 1) ozk_gemm_c64_kernel(
     OzkArgs a, const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmC) {
+  HQ_PDL_WAIT();
   constexpr int S = 7;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   // a_full: the M side's digits of a block landed; c_full: its FP64 N-side
@@ -1131,6 +1139,7 @@ __global__ void __launch_bounds__(NT, 1) ozk_gemm_c64_kernel(
 // (C += sign * A B^T) or 0 (C = sign * A B^T), no grid.z split.
 __global__ void __launch_bounds__(NT, 1) ozk_gemm_short_kernel(
     OzkArgs a, const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB) {
+  HQ_PDL_WAIT();
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   __shared__ __align__(8) uint64_t full_bar[MAX_STAGES], empty_bar[MAX_STAGES];
   __shared__ __align__(8) uint64_t tfull, tempty, done_bar;
@@ -1276,6 +1285,7 @@ __global__ void __launch_bounds__(NT, 1) ozk_gemm_short_kernel(
 
 __global__ void ozk_sum_slices(int M, int N, int Z, const double* __restrict__ ws,
                                double* __restrict__ C, long long crs, long long ccs, int accumulate) {
+  HQ_PDL_WAIT();
   const long long total = (long long)M * N;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
        e += (long long)gridDim.x * blockDim.x) {
@@ -1302,7 +1312,7 @@ extern "C" int hq_ozk_rowmax_raw(cudaStream_t stream, const double* X, long long
   if (R <= 0 || K <= 0) return 0;
   cudaError_t e = cudaMemsetAsync(raw, 0, sizeof(int) * (size_t)rows_total, stream);
   if (e != cudaSuccess) return (int)e;
-  ozk_rowmax_atomic_kernel<<<dim3(R, (K + ROWMAX_SPAN - 1) / ROWMAX_SPAN), 256, 0, stream>>>(
+  hq_launch(ozk_rowmax_atomic_kernel, dim3(R, (K + ROWMAX_SPAN - 1) / ROWMAX_SPAN), 256, 0, stream,
       X, rs, ks, K, raw);
   hq_count_launches(1);
   return (int)cudaGetLastError();
@@ -1336,14 +1346,14 @@ extern "C" int hq_ozk_split(cudaStream_t stream, const double* X, long long rs, 
     if (raw != nullptr) {  // row maxima with several CTAs per row (scratch given)
       const int e = hq_ozk_rowmax_raw(stream, X, rs, ks, R, K, rows_total, raw);
       if (e) return e;
-      ozk_split_chunk_kernel<7><<<(unsigned)cblocks, 256, 0, stream>>>(X, rs, ks, R, K, KB,
+      hq_launch(ozk_split_chunk_kernel<7>, (unsigned)cblocks, 256, 0, stream, X, rs, ks, R, K, KB,
                                                                         rows_total, t, exps, raw);
       hq_count_launches(1);
       return (int)cudaGetLastError();
     }
     int mblocks = rows_total < 8192 ? rows_total : 8192;
-    ozk_rowmax_kernel<<<mblocks, 256, 0, stream>>>(X, rs, ks, R, K, rows_total, exps);
-    ozk_split_chunk_kernel<7><<<(unsigned)cblocks, 256, 0, stream>>>(X, rs, ks, R, K, KB,
+    hq_launch(ozk_rowmax_kernel, mblocks, 256, 0, stream, X, rs, ks, R, K, rows_total, exps);
+    hq_launch(ozk_split_chunk_kernel<7>, (unsigned)cblocks, 256, 0, stream, X, rs, ks, R, K, KB,
                                                                       rows_total, t, exps, nullptr);
     hq_count_launches(2);
     return (int)cudaGetLastError();
@@ -1353,7 +1363,7 @@ extern "C" int hq_ozk_split(cudaStream_t stream, const double* X, long long rs, 
     switch (S) {
 #define HQ_SPLIT_CM_CASE(SS)                                                            \
   case SS:                                                                              \
-    ozk_split_cm_kernel<SS><<<cb, 256, 0, stream>>>(X, ks, R, K, KB, rows_total, t, exps); \
+    hq_launch(ozk_split_cm_kernel<SS>, cb, 256, 0, stream, X, ks, R, K, KB, rows_total, t, exps); \
     break;
       HQ_SPLIT_CM_CASE(1) HQ_SPLIT_CM_CASE(2) HQ_SPLIT_CM_CASE(3) HQ_SPLIT_CM_CASE(4)
       HQ_SPLIT_CM_CASE(5) HQ_SPLIT_CM_CASE(6) HQ_SPLIT_CM_CASE(7)
@@ -1364,7 +1374,7 @@ extern "C" int hq_ozk_split(cudaStream_t stream, const double* X, long long rs, 
   }
   if (K >= 4096 && K <= 512 * 8 * ROW_CPT && S == 7) {
     int rblocks = rows_total < 16384 ? rows_total : 16384;
-    ozk_split_row_kernel<7, ROW_CPT><<<rblocks, 512, 0, stream>>>(X, rs, ks, R, K, TR, KB,
+    hq_launch(ozk_split_row_kernel<7, ROW_CPT>, rblocks, 512, 0, stream, X, rs, ks, R, K, TR, KB,
                                                                  rows_total, t, exps);
     hq_count_launches(1);
     return (int)cudaGetLastError();
@@ -1372,7 +1382,7 @@ extern "C" int hq_ozk_split(cudaStream_t stream, const double* X, long long rs, 
   switch (S) {
 #define HQ_SPLIT_CASE(SS)                                                                  \
   case SS:                                                                                 \
-    ozk_split_kernel<SS><<<blocks, 256, 0, stream>>>(X, rs, ks, R, K, TR, KB, rows_total, t, \
+    hq_launch(ozk_split_kernel<SS>, blocks, 256, 0, stream, X, rs, ks, R, K, TR, KB, rows_total, t, \
                                                      exps);                                \
     break;
     HQ_SPLIT_CASE(1) HQ_SPLIT_CASE(2) HQ_SPLIT_CASE(3) HQ_SPLIT_CASE(4) HQ_SPLIT_CASE(5)
@@ -1398,7 +1408,7 @@ extern "C" int hq_ozk_split_raw(cudaStream_t stream, const double* X, long long 
   const long long chunks = (long long)rows_total * KB * (TK / 8);
   long long cblocks = (chunks + 255) / 256;
   if (cblocks > 65536) cblocks = 65536;
-  ozk_split_chunk_kernel<7><<<(unsigned)cblocks, 256, 0, stream>>>(
+  hq_launch(ozk_split_chunk_kernel<7>, (unsigned)cblocks, 256, 0, stream,
       X, rs, ks, R, K, KB, rows_total, static_cast<uint8_t*>(tiles), exps, raw);
   hq_count_launches(1);
   return (int)cudaGetLastError();
@@ -1515,13 +1525,13 @@ extern "C" int hq_ozk_gemm(cudaStream_t stream, const hq_device_info* dev, int M
   cudaError_t e =
       cudaFuncSetAttribute(ozk_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return (int)e;
-  ozk_gemm_kernel<<<dim3(MT, NTL, Z), NT, smem, stream>>>(a, tmA, tmB);
+  hq_launch(ozk_gemm_kernel, dim3(MT, NTL, Z), NT, smem, stream, a, tmA, tmB);
   hq_count_launches(1);
   if (Z > 1) {
     long long total = (long long)M * N;
     int blocks = (int)((total + 255) / 256);
     if (blocks > dev->num_sms * 8) blocks = dev->num_sms * 8;
-    ozk_sum_slices<<<blocks, 256, 0, stream>>>(M, N, Z, ws, C, crs, ccs, 0);
+    hq_launch(ozk_sum_slices, blocks, 256, 0, stream, M, N, Z, ws, C, crs, ccs, 0);
     hq_count_launches(1);
   }
   return (int)cudaGetLastError();
@@ -1606,13 +1616,13 @@ extern "C" int hq_ozk_gemm_c64(cudaStream_t stream, const hq_device_info* dev, i
   cudaError_t e = cudaFuncSetAttribute(ozk_gemm_c64_kernel,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return (int)e;
-  ozk_gemm_c64_kernel<<<dim3(MT, NTL, Z), NT, smem, stream>>>(a, tmA, tmC);
+  hq_launch(ozk_gemm_c64_kernel, dim3(MT, NTL, Z), NT, smem, stream, a, tmA, tmC);
   hq_count_launches(1);
   if (Z > 1) {
     long long total = (long long)M * N;
     int blocks = (int)((total + 255) / 256);
     if (blocks > dev->num_sms * 8) blocks = dev->num_sms * 8;
-    ozk_sum_slices<<<blocks, 256, 0, stream>>>(M, N, Z, ws, C, crs, ccs, 0);
+    hq_launch(ozk_sum_slices, blocks, 256, 0, stream, M, N, Z, ws, C, crs, ccs, 0);
     hq_count_launches(1);
   }
   return (int)cudaGetLastError();
@@ -1666,7 +1676,7 @@ extern "C" int hq_ozk_gemm_short(cudaStream_t stream, const hq_device_info* dev,
   if (e != cudaSuccess) return (int)e;
   const long long tiles = (long long)((M + TM - 1) / TM) * ((N + TNV - 1) / TNV);
   const int grid = (int)(tiles < dev->num_sms ? tiles : dev->num_sms);
-  ozk_gemm_short_kernel<<<grid, NT, smem, stream>>>(a, tmA, tmB);
+  hq_launch(ozk_gemm_short_kernel, grid, NT, smem, stream, a, tmA, tmB);
   hq_count_launches(1);
   return (int)cudaGetLastError();
 }

@@ -19,6 +19,7 @@ __global__ void gather_pairs(int rows, const double* __restrict__ X, int ldx,
                              const int* __restrict__ pairs, const int* __restrict__ npairs,
                              int ncols, double* __restrict__ tmp,
                              const int* __restrict__ labels, int* __restrict__ label_tmp) {
+  HQ_PDL_WAIT();
   const int p = blockIdx.y;
   if (p >= *npairs) return;
   const int src = pairs[2 * p + 1];
@@ -34,6 +35,7 @@ __global__ void scatter_pairs(int rows, double* __restrict__ X, int ldx,
                               const int* __restrict__ pairs, const int* __restrict__ npairs,
                               int ncols, const double* __restrict__ tmp,
                               int* __restrict__ labels, const int* __restrict__ label_tmp) {
+  HQ_PDL_WAIT();
   const int p = blockIdx.y;
   if (p >= *npairs) return;
   const int dst = pairs[2 * p];
@@ -48,6 +50,7 @@ __global__ void scatter_pairs(int rows, double* __restrict__ X, int ldx,
 __global__ void gather_perm(int rows, const double* __restrict__ X, int ldx,
                             const int* __restrict__ perm, double* __restrict__ tmp,
                             const int* __restrict__ labels, int* __restrict__ label_tmp) {
+  HQ_PDL_WAIT();
   const int k = blockIdx.y;
   const int src = perm[k];
   // A column that stays in place is neither gathered nor scattered.
@@ -62,6 +65,7 @@ __global__ void gather_perm(int rows, const double* __restrict__ X, int ldx,
 __global__ void scatter_perm(int rows, double* __restrict__ X, int ldx,
                              const int* __restrict__ perm, const double* __restrict__ tmp,
                              int* __restrict__ labels, const int* __restrict__ label_tmp) {
+  HQ_PDL_WAIT();
   const int k = blockIdx.y;
   if (perm[k] < 0 || perm[k] >= (int)gridDim.y || perm[k] == k) return;
   double* d = X + (size_t)k * ldx;
@@ -72,12 +76,14 @@ __global__ void scatter_perm(int rows, double* __restrict__ X, int ldx,
 }
 
 __global__ void iota_kernel(int* x, int n, int base) {
+  HQ_PDL_WAIT();
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     x[i] = base + i;
 }
 
 __global__ void copy_kernel(int rows, int cols, const double* __restrict__ src, int lds,
                             double* __restrict__ dst, int ldd) {
+  HQ_PDL_WAIT();
   const size_t total = (size_t)rows * cols;
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total;
        e += (size_t)gridDim.x * blockDim.x) {
@@ -100,8 +106,8 @@ extern "C" int hq_permute_pairs(cudaStream_t stream, int rows, double* X, int ld
   if (max_pairs <= 0 || (rows <= 0 && labels == nullptr)) return 0;
   const int r = rows > 0 ? rows : 0;
   dim3 grid(row_blocks(r), max_pairs);
-  gather_pairs<<<grid, 256, 0, stream>>>(r, X, ldx, pairs, npairs, ncols, tmp, labels, label_tmp);
-  scatter_pairs<<<grid, 256, 0, stream>>>(r, X, ldx, pairs, npairs, ncols, tmp, labels,
+  hq_launch(gather_pairs, grid, 256, 0, stream, r, X, ldx, pairs, npairs, ncols, tmp, labels, label_tmp);
+  hq_launch(scatter_pairs, grid, 256, 0, stream, r, X, ldx, pairs, npairs, ncols, tmp, labels,
                                            label_tmp);
   hq_count_launches(2);
   return (int)cudaGetLastError();
@@ -112,15 +118,15 @@ extern "C" int hq_permute_cols(cudaStream_t stream, int rows, double* X, int ldx
   if (nc <= 0 || (rows <= 0 && labels == nullptr)) return 0;
   const int r = rows > 0 ? rows : 0;
   dim3 grid(row_blocks(r), nc);
-  gather_perm<<<grid, 256, 0, stream>>>(r, X, ldx, perm, tmp, labels, label_tmp);
-  scatter_perm<<<grid, 256, 0, stream>>>(r, X, ldx, perm, tmp, labels, label_tmp);
+  hq_launch(gather_perm, grid, 256, 0, stream, r, X, ldx, perm, tmp, labels, label_tmp);
+  hq_launch(scatter_perm, grid, 256, 0, stream, r, X, ldx, perm, tmp, labels, label_tmp);
   hq_count_launches(2);
   return (int)cudaGetLastError();
 }
 
 extern "C" int hq_fill_iota(cudaStream_t stream, int* x, int n, int base) {
   if (n <= 0) return 0;
-  iota_kernel<<<(n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024, 256, 0, stream>>>(x, n, base);
+  hq_launch(iota_kernel, (n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024, 256, 0, stream, x, n, base);
   hq_count_launches(1);
   return (int)cudaGetLastError();
 }
@@ -131,7 +137,7 @@ extern "C" int hq_copy_matrix(cudaStream_t stream, int rows, int cols, const dou
   size_t total = (size_t)rows * cols;
   size_t blocks = (total + 255) / 256;
   if (blocks > 4096) blocks = 4096;
-  copy_kernel<<<(unsigned)blocks, 256, 0, stream>>>(rows, cols, src, lds, dst, ldd);
+  hq_launch(copy_kernel, (unsigned)blocks, 256, 0, stream, rows, cols, src, lds, dst, ldd);
   hq_count_launches(1);
   return (int)cudaGetLastError();
 }
@@ -141,6 +147,12 @@ static unsigned long long g_launches = 0;
 extern "C" void hq_count_launches(int k) { __atomic_add_fetch(&g_launches, (unsigned long long)k, __ATOMIC_RELAXED); }
 
 extern "C" unsigned long long hq_launches(void) { return __atomic_load_n(&g_launches, __ATOMIC_RELAXED); }
+
+static int g_pdl = 1;
+
+extern "C" void hq_set_pdl(int on) { __atomic_store_n(&g_pdl, on ? 1 : 0, __ATOMIC_RELAXED); }
+
+extern "C" int hq_pdl(void) { return __atomic_load_n(&g_pdl, __ATOMIC_RELAXED); }
 
 extern "C" int hq_query_device(hq_device_info* info) {
   int dev = 0;

@@ -87,6 +87,7 @@ __global__ void __launch_bounds__(CT, 1)
     gram_pchol32_kernel(int n, const double* __restrict__ G, int ldg, double* __restrict__ R,
                         int ldr, int* __restrict__ perm, int* __restrict__ stat, int bit,
                         int* __restrict__ alt, unsigned long long* __restrict__ emax) {
+  HQ_PDL_WAIT();
   extern __shared__ float s_Rp[];  // GN * GN: s_Rp[k * GN + i] = row k of Rs at source column i
   __shared__ double s_sc[GN], s_rt[GN];
   __shared__ float s_key[GN], s_d[GN], s_l[GN], s_r[GN], s_wmax[CW];
@@ -289,6 +290,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CLT, 1)
                         double* __restrict__ F, int ldf, double* __restrict__ dsgn,
                         double* __restrict__ tau, int* __restrict__ stat, int bit,
                         const int* __restrict__ gate) {
+  HQ_PDL_WAIT();
   if (gate != nullptr && *gate == 0) return;  // every CTA of the cluster reads the same word
   cg::cluster_group cl = cg::this_cluster();
   const int rank = (int)cl.block_rank();
@@ -458,6 +460,7 @@ __global__ void __launch_bounds__(TW * 32)
                   const double* __restrict__ Zin, int ld, double* __restrict__ Xout,
                   double* __restrict__ Zout, int it, int* __restrict__ alt,
                   unsigned long long* __restrict__ emax) {
+  HQ_PDL_WAIT();
   extern __shared__ double sX[];  // LDS * n: X's columns 0..c, rows <= column
   __shared__ double s_z[GN];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -571,6 +574,7 @@ struct TriJob {
 // pipe on one dependent chain.
 __global__ void __launch_bounds__(TW * 32)
     tri_kernel(int n, TriJob j0, TriJob j1, const int* __restrict__ gate) {
+  HQ_PDL_WAIT();
   extern __shared__ double sA[];  // LDS * n
   __shared__ double s_dinv[GN];
   if (gate != nullptr && *gate == 0) return;
@@ -673,6 +677,7 @@ __global__ void gram_commit_kernel(int mp, int n, double* __restrict__ P, int ld
                                    const double* __restrict__ tau_in, double* __restrict__ tau,
                                    int* __restrict__ perm, const int* __restrict__ stat,
                                    int* __restrict__ count) {
+  HQ_PDL_WAIT();
   const int st = *stat;
   if (count != nullptr && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0)
     atomicAdd(&count[st != 0 ? 1 : 0], 1);
@@ -714,7 +719,7 @@ extern "C" int hq_gram_pchol32(cudaStream_t stream, int n, const double* G, int 
   cudaError_t e = cudaFuncSetAttribute(gram_pchol32_kernel,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return (int)e;
-  gram_pchol32_kernel<<<1, CT, smem, stream>>>(n, G, ldg, R, ldr, perm, stat, bit, alt,
+  hq_launch(gram_pchol32_kernel, 1, CT, smem, stream, n, G, ldg, R, ldr, perm, stat, bit, alt,
                                                 emax);
   hq_count_launches(1);
   return (int)cudaGetLastError();
@@ -724,7 +729,7 @@ extern "C" int hq_cluster_fact(cudaStream_t stream, int n, int mode, const doubl
                                double* F, int ldf, double* dsgn, double* tau, int* stat, int bit,
                                const int* gate) {
   if (n <= 0 || n > GN || mode < 0 || mode > 1) return (int)cudaErrorInvalidValue;
-  cluster_fact_kernel<<<CL, CLT, 0, stream>>>(n, mode, A, lda, F, ldf, dsgn, tau, stat, bit,
+  hq_launch(cluster_fact_kernel, CL, CLT, 0, stream, n, mode, A, lda, F, ldf, dsgn, tau, stat, bit,
                                               gate);
   hq_count_launches(1);
   return (int)cudaGetLastError();
@@ -745,7 +750,7 @@ extern "C" int hq_nearid_chol(cudaStream_t stream, int n, const double* G, int l
     const double* zi = (it & 1) ? wZ : Rinv;
     double* xo = (it & 1) ? R : wX;
     double* zo = (it & 1) ? Rinv : wZ;
-    nearid_kernel<<<n, TW * 32, smem, stream>>>(n, G, ldg, xi, zi, ld, xo, zo, it, alt, emax);
+    hq_launch(nearid_kernel, n, TW * 32, smem, stream, n, G, ldg, xi, zi, ld, xo, zo, it, alt, emax);
   }
   hq_count_launches(NEARID_ITERS);
   return (int)cudaGetLastError();
@@ -779,7 +784,7 @@ extern "C" int hq_tri2g(cudaStream_t stream, int n, int mode0, const double* A0,
   if (e != cudaSuccess) return (int)e;
   const TriJob j0 = {mode0, A0, lda0, B0, ldb0, rs0, X0, ldx0};
   const TriJob j1 = {mode1 < 0 ? 0 : mode1, A1, lda1, B1, ldb1, rs1, X1, ldx1};
-  tri_kernel<<<mode1 < 0 ? n : 2 * n, TW * 32, smem, stream>>>(n, j0, j1, gate);
+  hq_launch(tri_kernel, mode1 < 0 ? n : 2 * n, TW * 32, smem, stream, n, j0, j1, gate);
   hq_count_launches(1);
   return (int)cudaGetLastError();
 }
@@ -791,7 +796,7 @@ extern "C" int hq_gram_commit(cudaStream_t stream, int mp, int n, double* P, int
   if (mp <= 0 || n <= 0) return 0;
   int bx = (mp + 255) / 256;
   if (bx > 64) bx = 64;
-  gram_commit_kernel<<<dim3(bx, n), 256, 0, stream>>>(mp, n, P, ldp, U, ldu, RH, ldr, LU, ldlu,
+  hq_launch(gram_commit_kernel, dim3(bx, n), 256, 0, stream, mp, n, P, ldp, U, ldu, RH, ldr, LU, ldlu,
                                                       tau_in, tau, perm, stat, count);
   hq_count_launches(1);
   return (int)cudaGetLastError();

@@ -44,6 +44,7 @@ __device__ __forceinline__ void philox4x32_10(uint64_t counter, uint64_t seed, u
 
 __global__ void sketch_philox_kernel(int rows, int cols, double* __restrict__ G, int ldg,
                                      uint64_t seed) {
+  HQ_PDL_WAIT();
   const uint64_t total = (uint64_t)rows * cols;
   const uint64_t pairs = (total + 1) / 2;
   for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < pairs;
@@ -79,7 +80,7 @@ extern "C" int hq_sketch_philox(cudaStream_t stream, int rows, int cols, double*
   const uint64_t pairs = ((uint64_t)rows * cols + 1) / 2;
   uint64_t blocks = (pairs + 255) / 256;
   if (blocks > 4096) blocks = 4096;
-  sketch_philox_kernel<<<(unsigned)blocks, 256, 0, stream>>>(rows, cols, G, ldg, seed);
+  hq_launch(sketch_philox_kernel, (unsigned)blocks, 256, 0, stream, rows, cols, G, ldg, seed);
   hq_count_launches(1);
   return (int)cudaGetLastError();
 }
