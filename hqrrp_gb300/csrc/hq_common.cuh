@@ -40,6 +40,33 @@ static inline void hq_launch(void (*kernel)(KArgs...), dim3 grid, dim3 block, si
   (void)cudaLaunchKernelEx(&cfg, kernel, static_cast<Args&&>(args)...);
 }
 
+// Cooperative launch (every CTA co-resident, as the grid barriers need), with
+// programmatic dependent launch as above; the kernel begins with
+// HQ_PDL_WAIT().  Should the runtime refuse the two attributes together, the
+// launch is repeated as a plain cooperative launch.
+static inline cudaError_t hq_launch_coop(const void* kernel, dim3 grid, dim3 block, void** args,
+                                         size_t smem, cudaStream_t stream) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[2];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[1].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = hq_pdl() ? 2 : 1;
+  cudaError_t e = cudaLaunchKernelExC(&cfg, kernel, args);
+  if (e != cudaSuccess && cfg.numAttrs == 2) {
+    (void)cudaGetLastError();
+    cfg.numAttrs = 1;
+    e = cudaLaunchKernelExC(&cfg, kernel, args);
+  }
+  return e;
+}
+
 __device__ __forceinline__ unsigned hq_ld_acquire(const unsigned* p) {
   unsigned v;
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");

@@ -244,6 +244,9 @@ int hq_copy_matrix(cudaStream_t stream, int rows, int cols, const double* src, i
  * HQRRP_GB300_PDL=0 (read by each call's workspace setup). */
 void hq_set_pdl(int on);
 int hq_pdl(void);
+/* Zero two word arrays (n1, n2 32-bit words; p2 may be NULL) in one launch
+ * that keeps the programmatic-launch chain (a memset node breaks it). */
+int hq_zero_words(cudaStream_t stream, void* p1, size_t n1, void* p2, size_t n2);
 
 #ifdef __cplusplus
 }

@@ -542,14 +542,18 @@ static int ozk_product_x(hq_ws* w, int S, int M, int N, int K, const double* X, 
   const int* ae = xt ? xe : w->ozea;
   const int ovr = w->ph_override;
   const int yside = short_k ? 2 : 1;
-  if (!xt && !y_raw && X == Y && xrs == yrs && xks == yks && M == N && S == OZK_SLICES &&
-      K >= 512 && w->ozraw) {
+  if (!xt && X == Y && xrs == yrs && xks == yks && M == N && S == OZK_SLICES && K >= 512 &&
+      (y_raw || w->ozraw)) {
     /* A Gram product (both operands the same matrix): one pass of row maxima
-     * for both splits. */
-    const int rt = imax(hq_ozk_split_rows(M, 0), hq_ozk_split_rows(N, yside));
-    CK(hq_ozk_rowmax_raw(w->st, X, xrs, xks, M, K, rt, w->ozraw));
-    CK(hq_ozk_split_raw(w->st, X, xrs, xks, M, K, S, 0, w->ozA, w->ozea, w->ozraw));
-    CK(hq_ozk_split_raw(w->st, Y, yrs, yks, N, K, S, yside, w->ozB, w->ozeb, w->ozraw));
+     * for both splits, or none when they are known (y_raw). */
+    const int* raw = y_raw;
+    if (!raw) {
+      const int rt = imax(hq_ozk_split_rows(M, 0), hq_ozk_split_rows(N, yside));
+      CK(hq_ozk_rowmax_raw(w->st, X, xrs, xks, M, K, rt, w->ozraw));
+      raw = w->ozraw;
+    }
+    CK(hq_ozk_split_raw(w->st, X, xrs, xks, M, K, S, 0, w->ozA, w->ozea, raw));
+    CK(hq_ozk_split_raw(w->st, Y, yrs, yks, N, K, S, yside, w->ozB, w->ozeb, raw));
   } else {
     if (!xt) CK(hq_ozk_split(w->st, X, xrs, xks, M, K, S, 0, w->ozA, w->ozea, w->ozraw));
     if (y_raw)
@@ -670,13 +674,16 @@ static int drain_finish(hq_ws* w, double* host, int lda, const double* dev, int 
  * every step succeeded (*gstat == 0), and otherwise the cooperative panel
  * that follows on the stream factors the (permuted) panel itself. */
 static int gram_panel(hq_ws* w, int m, int j, int b, int piv, double* AR, int ldda, int* jp,
-                      double* tau) {
+                      double* tau, const int* raw) {
   const int mp = m - j, L = HQ_GRAM_MAX, S = OZK_SLICES;
   double* ABR = AR + j;
   int rc;
   w->ph_override = PH_PANEL;
-  /* G = Ap^T Ap; R1, P (pivoted Cholesky); R1^{-1} */
-  rc = ozk_product(w, S, b, b, mp, ABR, ldda, 1, ABR, ldda, 1, 0, 1.0, w->gG, 1, L);
+  /* G = Ap^T Ap; R1, P (pivoted Cholesky); R1^{-1}.  raw: the panel
+   * columns' largest exponent fields over rows >= j, when the previous
+   * block's update recorded them (its product needs no row-maximum pass). */
+  rc = ozk_product_x(w, S, b, b, mp, ABR, ldda, 1, ABR, ldda, 1, 0, 1.0, w->gG, 1, L, raw, NULL,
+                     0, NULL, NULL);
   if (rc) return rc;
   if (piv) {
     CK(hq_gram_pchol32(w->st, b, w->gG, L, w->gR1, L, w->gperm, w->gstat, 1, w->galt,
@@ -768,7 +775,7 @@ static int block_reflector(hq_ws* w, int mp, int b, const double* tau, double* C
     rc = ozk_product(w, OZK_SLICES, b, nc2, b, w->T, w->ldt, 1, w->W1, w->ldw, 1, 0, 1.0, w->W2, 1,
                      w->ldw);
     if (rc) return rc;
-    if (cx_out) CK(cudaMemsetAsync(cx_out, 0, sizeof(int) * (size_t)nc2, w->st));
+    if (cx_out) CK(hq_zero_words(w->st, cx_out, (size_t)nc2, NULL, 0));
     rc = ozk_product_x(w, OZK_SLICES, mp, nc2, b, w->U, 1, w->ldu, w->W2, w->ldw, 1, 1, -1.0, Cm,
                        1, ldc, NULL, cx_out, b, w->ozU, w->ozUe);
     if (rc) return rc;
@@ -816,6 +823,10 @@ static int core_hqrrp_k(hq_ws* w, int m, int n, double* dA, int ldda, int* djpvt
   NV_POP();
 
   int cx_ok = 0; /* w->colexp holds the trailing columns' exponent fields */
+  /* HQRRP_GB300_SPLIT_TRAILING=1: the separate split and row-maximum passes
+   * everywhere (the same digits; for verification). */
+  const char* split_env = getenv("HQRRP_GB300_SPLIT_TRAILING");
+  const int split_passes = split_env && split_env[0] == '1';
   for (int j = 0; j < mn; j += nb) {
     const int b = imin(imin(nb, mn - j), imin(n - j, m - j));
     const int last = (j + nb >= m) || (j + nb >= n);
@@ -849,7 +860,8 @@ static int core_hqrrp_k(hq_ws* w, int m, int n, double* dA, int ldda, int* djpvt
      * LAWN 176 downdate); plain keeps LAPACK's formula. */
     const int use_gram = w->gram && w->gQ && !w->ut && b <= HQ_GRAM_MAX;
     if (use_gram) {
-      int rc = gram_panel(w, m, j, b, panel_piv, AR, ldda, djpvt + j, dtau + j);
+      int rc = gram_panel(w, m, j, b, panel_piv, AR, ldda, djpvt + j, dtau + j,
+                          cx_ok && !split_passes ? w->colexp + j : NULL);
       if (rc) return rc;
     }
     CK(hq_panel_qrp_fallback(w->st, dev, mp, b, panel_piv, ABR, ldda, dtau + j, w->U, w->ldu,

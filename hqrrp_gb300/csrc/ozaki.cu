@@ -1310,8 +1310,8 @@ extern "C" size_t hq_ozk_tile_bytes(int rows, int K, int S, int side) {
 extern "C" int hq_ozk_rowmax_raw(cudaStream_t stream, const double* X, long long rs,
                                  long long ks, int R, int K, int rows_total, int* raw) {
   if (R <= 0 || K <= 0) return 0;
-  cudaError_t e = cudaMemsetAsync(raw, 0, sizeof(int) * (size_t)rows_total, stream);
-  if (e != cudaSuccess) return (int)e;
+  const int e = hq_zero_words(stream, raw, (size_t)rows_total, nullptr, 0);
+  if (e) return e;
   hq_launch(ozk_rowmax_atomic_kernel, dim3(R, (K + ROWMAX_SPAN - 1) / ROWMAX_SPAN), 256, 0, stream,
       X, rs, ks, K, raw);
   hq_count_launches(1);

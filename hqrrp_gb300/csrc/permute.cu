@@ -75,6 +75,16 @@ __global__ void scatter_perm(int rows, double* __restrict__ X, int ldx,
   if (labels && blockIdx.x == 0 && threadIdx.x == 0) labels[k] = label_tmp[k];
 }
 
+__global__ void zero_words_kernel(unsigned* __restrict__ p1, long long n1, unsigned* __restrict__ p2,
+                                  long long n2) {
+  HQ_PDL_WAIT();
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n1 + n2; i += stride) {
+    if (i < n1) p1[i] = 0u;
+    else p2[i - n1] = 0u;
+  }
+}
+
 __global__ void iota_kernel(int* x, int n, int base) {
   HQ_PDL_WAIT();
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
@@ -121,6 +131,18 @@ extern "C" int hq_permute_cols(cudaStream_t stream, int rows, double* X, int ldx
   hq_launch(gather_perm, grid, 256, 0, stream, r, X, ldx, perm, tmp, labels, label_tmp);
   hq_launch(scatter_perm, grid, 256, 0, stream, r, X, ldx, perm, tmp, labels, label_tmp);
   hq_count_launches(2);
+  return (int)cudaGetLastError();
+}
+
+extern "C" int hq_zero_words(cudaStream_t stream, void* p1, size_t n1, void* p2, size_t n2) {
+  if (p2 == nullptr) n2 = 0;
+  const size_t total = n1 + n2;
+  if (total == 0) return 0;
+  size_t blocks = (total + 255) / 256;
+  if (blocks > 1024) blocks = 1024;
+  hq_launch(zero_words_kernel, (unsigned)blocks, 256, 0, stream, static_cast<unsigned*>(p1),
+            (long long)n1, static_cast<unsigned*>(p2), (long long)n2);
+  hq_count_launches(1);
   return (int)cudaGetLastError();
 }
 

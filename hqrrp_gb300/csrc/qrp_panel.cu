@@ -105,6 +105,7 @@ __device__ __forceinline__ void pick(long long key, int k, long long& bkey, int&
 }
 
 __global__ void __launch_bounds__(NT, 1) panel_qrp_kernel(PnArgs a) {
+  HQ_PDL_WAIT();
   extern __shared__ __align__(16) double smem[];
   // Every CTA reads the same word, written before the launch.
   if (a.gram_stat != nullptr && *a.gram_stat == 0) return;
@@ -623,10 +624,10 @@ extern "C" int hq_panel_qrp_fallback(cudaStream_t stream, const hq_device_info* 
   cudaError_t e = cudaFuncSetAttribute(panel_qrp_kernel,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return (int)e;
-  if ((e = cudaMemsetAsync(bar, 0, sizeof(unsigned), stream)) != cudaSuccess) return (int)e;
+  const int z = hq_zero_words(stream, bar, 1, nullptr, 0);
+  if (z) return z;
   void* args[] = {&a};
-  e = cudaLaunchCooperativeKernel((const void*)panel_qrp_kernel, dim3(G), dim3(NT), args, smem,
-                                  stream);
+  e = hq_launch_coop((const void*)panel_qrp_kernel, dim3(G), dim3(NT), args, smem, stream);
   hq_count_launches(1);
   return (int)e;
 }

@@ -54,6 +54,7 @@ __device__ __forceinline__ bool better(double d1, int p1, double d2, int p2) {
 }
 
 __global__ void __launch_bounds__(NT, 1) skinny_qrp_kernel(SkArgs a) {
+  HQ_PDL_WAIT();
   extern __shared__ __align__(16) double smem[];
   const int P = gridDim.x, cta = blockIdx.x, tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
@@ -294,6 +295,7 @@ __device__ __forceinline__ bool better_key(long long k1, int p1, long long k2, i
 
 template <int RPT, typename T>
 __global__ void __launch_bounds__(NT, 1) skinny_qrp_reg_kernel(SkArgs a) {
+  HQ_PDL_WAIT();
   constexpr int NCH = RPT / 8;  // chunks of 8 registers = 16 rows
   constexpr bool SQ = sizeof(T) == 4;  // mixed path: squared norms
   constexpr int NC = NT / 2;
@@ -665,8 +667,8 @@ extern "C" int hq_skinny_qrp(cudaStream_t stream, const hq_device_info* dev, int
     if (V == nullptr || smem > dev->smem_optin) return (int)cudaErrorInvalidValue;
   }
   cudaError_t e;
-  if ((e = cudaMemsetAsync(bar, 0, sizeof(unsigned), stream)) != cudaSuccess) return (int)e;
-  if ((e = cudaMemsetAsync(npairs, 0, sizeof(int), stream)) != cudaSuccess) return (int)e;
+  const int z = hq_zero_words(stream, bar, 1, npairs, 1);
+  if (z) return z;
   void* args[] = {&a};
   const void* fn = nullptr;
   const bool reg_ok = a.nloc_max <= NT / 2 && P <= 160;  // 5 records per lane in the winner pick
@@ -675,13 +677,12 @@ extern "C" int hq_skinny_qrp(cudaStream_t stream, const hq_device_info* dev, int
   else if (reg_ok && mY <= 2 * 72)
     fn = fp32 ? (const void*)skinny_qrp_reg_kernel<72, float> : (const void*)skinny_qrp_reg_kernel<72, double>;
   if (fn != nullptr) {
-    e = cudaLaunchCooperativeKernel(fn, dim3(P), dim3(NT), args, 0, stream);
+    e = hq_launch_coop(fn, dim3(P), dim3(NT), args, 0, stream);
   } else {
     e = cudaFuncSetAttribute(skinny_qrp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem);
     if (e != cudaSuccess) return (int)e;
-    e = cudaLaunchCooperativeKernel((const void*)skinny_qrp_kernel, dim3(P), dim3(NT), args, smem,
-                                    stream);
+    e = hq_launch_coop((const void*)skinny_qrp_kernel, dim3(P), dim3(NT), args, smem, stream);
   }
   hq_count_launches(1);
   return (int)e;

@@ -125,8 +125,10 @@ def test_mixed_dgeqp4_small_path_fixed_columns(mixed, m, n, every):
 def test_trailing_digits_cut_on_the_fly_are_the_split_digits(hq, m, n, nb):
     """From the second block on, W1 = U'^T C reads C as FP64 and cuts its
     digits in shared memory (scales from the previous update's column
-    exponents) instead of a separate split pass: the digits are the same, so
-    the factorization is bit-identical to the split path's."""
+    exponents) instead of a separate split pass, and the Gram panel's
+    G = Ap^T Ap takes the same recorded exponents instead of a row-maximum
+    pass: the digits are the same, so the factorization is bit-identical to
+    the separate passes' (HQRRP_GB300_SPLIT_TRAILING=1)."""
     import os
     A = oracle.gaussian(m, n, m + 2 * n)
     prev = hq.set_precision(hq.MIXED)
