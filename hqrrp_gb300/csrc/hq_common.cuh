@@ -99,12 +99,15 @@ __device__ __forceinline__ long long hq_norm_key(double d) {
 // Bounded grid barrier.  `counter` is zeroed before the launch; barrier number
 // `epoch` (1-based) completes when the counter reaches epoch * nctas.  Returns
 // false (in every thread of the CTA) if the wait gave up or another CTA
-// reported an error; the caller must then leave the kernel.
+// reported an error; the caller must then leave the kernel.  Ordering: the
+// CTA's writes before the barrier reach thread 0 through __syncthreads, and
+// its release add at GPU scope carries them (release is cumulative) to every
+// CTA whose acquire load reads the completed count; __syncthreads passes them
+// on to that CTA's threads.  No sequentially consistent fence is needed.
 __device__ __forceinline__ bool hq_grid_barrier(unsigned* counter, int* err, unsigned epoch,
                                                 unsigned spin_limit, int* s_flag) {
   __syncthreads();
   if (threadIdx.x == 0) {
-    __threadfence();
     hq_red_release_add(counter, 1u);
     const unsigned target = epoch * gridDim.x;
     unsigned spins = 0;
